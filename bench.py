@@ -1,0 +1,364 @@
+"""Benchmark of the per-step gravity solve on GB300; prints ONE JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload bh|pp] [--impl ours|reference]
+
+Workloads (seeded synthetic inputs with the shapes the configurations name;
+no public dataset is involved):
+  pp : direct sum, N = 16,384 bodies uniform in a ball of radius 100, masses
+       U[1, 10), v = 0, dt = 0.0035, eps^2 = 40 (the reference's -v 2 path).
+       Metric: interactions/s (N^2 per step, 20 flop each by convention).
+
+A "step" is one ParticleSolver::updateParticlePositions: forces + integrator.
+value: K steps on HBM-resident state, timed with CUDA events on the launch
+stream, L2 flushed (a 256 MiB write) between steps outside the event pair.
+e2e:   the same steps through the C ABI's host-layout call (nbody_update_host)
+with pinned host buffers, every step copying the reference layout in and out.
+Multi-GPU: the path is replicated, not sharded ("replicas only"): under
+torchrun every rank steps its own copy and value sums the ranks' work.
+
+--impl reference times the reference's own CPU implementation of the path on
+the host cores (the reference sources compiled headless when they are present
+here, else this project's pinned C restatement of them), same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "n-body_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "PP interactions/s (%FP32 peak), BH body-steps/s; served sims/s + p99 vs plain"
+PP_N, PP_DT, PP_EPS2 = 16384, 0.0035, 40.0
+FLOP_PER_INTERACTION = 20
+L2_FLUSH_BYTES = 256 << 20
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        d["source"] = "measured"
+        return d
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0, "source": "fallback"}
+
+
+def fp32_peak_tflops(sms: int, mhz: float) -> float:
+    # 128 FP32 lanes per SM, an FMA counts 2 flop
+    return sms * 128 * 2 * mhz * 1e6 / 1e12
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) taken while the GPU is under load."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.dev)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def init_dist(world, local):
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        return dist
+    return None
+
+
+def max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def profile_traffic(kernel: str):
+    """DRAM bytes per launch from a committed ncu summary (profiles/<kernel>*.md), if any."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for fn in sorted(os.listdir(pdir)):
+        if fn.startswith(kernel) and fn.endswith(".md"):
+            with open(os.path.join(pdir, fn)) as f:
+                m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read())
+            if m:
+                return float(m.group(1))
+    return None
+
+
+# ------------------------------------------------------------------ PP (ours)
+def bench_pp(args, world, rank, local, dist):
+    import torch
+
+    import nbody_gb300 as nb
+    from nbody_gb300 import initializers as I
+
+    torch.cuda.set_device(local)
+    n = PP_N
+    pos, vel, mass = I.uniform_ball(n, seed=12345 + rank)
+    system = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+    solver = nb.ParticleSolverCUDA(PP_DT, PP_EPS2, n, mode="pp", device=local)
+    stream = torch.cuda.current_stream()
+    solver.set_stream(stream.cuda_stream)
+    solver.upload(system)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    cfg = solver.pp_config()
+    launches_per_step = 1 + (1 if cfg["slices"] > 1 else 0)
+
+    def timed_steps(k, profile=False):
+        evs = []
+        for _ in range(k):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            solver.step(1)
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in evs)
+
+    # warm-up (untimed), then a short soak so that the clock samples cover load
+    timed_steps(max(3, args.warmup))
+    sampler = ClockSampler(local)
+    sampler.start()
+    t_end = time.time() + 1.5
+    while time.time() < t_end:
+        timed_steps(20)
+    barrier(dist)
+    torch.cuda.synchronize()
+    ms = timed_steps(args.steps)
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = max_over_ranks(dist, ms)
+    sec = ms / 1e3
+    interactions = float(n) * n * args.steps * world
+    value = interactions / sec
+
+    # dominant kernel alone: per-stage CUDA events on the launch stream
+    solver.profile_enable(True)
+    timed_steps(args.steps)
+    prof = solver.profile_read()
+    solver.profile_enable(False)
+    f_ms, f_cnt = prof.get("pp_force", (0.0, 0))
+    per_launch_s = f_ms / 1e3 / max(1, f_cnt)
+    achieved_tflops = FLOP_PER_INTERACTION * float(n) * n / per_launch_s / 1e12
+    pk = peaks()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    peak = fp32_peak_tflops(sms, float(pk.get("sm_max_mhz", 2070.0)))
+    roofline = {"bound": "fp32", "achieved": round(achieved_tflops, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
+                "frac": round(achieved_tflops / peak, 4), "traffic": profile_traffic("pp_force"),
+                "kernel": "pp_force_kernel", "kernel_ms_per_launch": round(per_launch_s * 1e3, 5),
+                "peak_note": f"nominal FP32 FMA peak {sms} SMs x 128 lanes x 2 flop x {pk.get('sm_max_mhz')} MHz "
+                             f"(max SM clock of {pk['source']} peaks file; no FP32 figure is measured there)",
+                "stage_ms": {k: round(v[0] / max(1, v[1]), 5) for k, v in prof.items()}}
+    if clocks.get("sm_mhz"):
+        roofline["frac_at_median_clock"] = round(achieved_tflops / fp32_peak_tflops(sms, clocks["sm_mhz"]), 4)
+
+    # end to end through the reference-facing call with pinned host buffers
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    hsys = nb.ParticleSystem(pin(pos.copy()), pin(vel.copy()), mass)
+    hsys.masses = pin(hsys.masses)
+    hsys.forces = pin(hsys.forces)
+    hsys.accelerations = pin(hsys.accelerations)
+    for _ in range(3):
+        solver.update_particle_positions(hsys)
+    torch.cuda.synchronize()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        solver.update_particle_positions(hsys)
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e = {"value": interactions / e2e_s, "unit": "interactions/s", "h2d_bytes_per_step": 4 * 16 * n,
+           "d2h_bytes_per_step": 4 * 16 * n, "ms_per_step": round(e2e_s * 1e3 / args.steps, 4),
+           "api": "nbody_update_host (ParticleSolver::updateParticlePositions)"}
+
+    line = {"metric": METRIC, "component": "PP interactions/s", "value": value, "unit": "interactions/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "direct-sum PP, N=16384 uniform ball R=100, m~U[1,10), v=0, dt=0.0035, "
+                                   "eps2=40 (reference -v 2 path)", "n_bodies": n, "parallelism": "replicas",
+                       "l2": "flushed between steps (256 MiB write, outside the event pair)",
+                       "pp_launch": cfg},
+            "clocks": clocks, "roofline": roofline, "e2e": e2e,
+            "gpu_launches": launches_per_step * args.steps,
+            "tflops_20flop": FLOP_PER_INTERACTION * interactions / sec / 1e12}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_pp()
+    solver.close()
+    return line
+
+
+def cpu_kind():
+    import pyoracle
+
+    return "reference" if pyoracle.ref_available() else "port"
+
+
+def cpu_threads():
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+
+def cpu_pp_step_seconds(pos, vel, mass, steps, threads):
+    import pyoracle
+
+    acc = np.zeros_like(pos)
+    if pyoracle.ref_available():
+        return pyoracle.ref_run(2, pos, vel, acc, mass, PP_DT, PP_EPS2, steps, threads=threads)[4]["seconds"]
+    return pyoracle.pp_run(pos, vel, acc, mass, PP_DT, PP_EPS2, steps, threads=threads)[4]
+
+
+def cpu_baseline_pp(budget_s: float = 12.0):
+    import pyoracle
+    from nbody_gb300 import initializers as I
+
+    pyoracle.build(reference=False)
+    threads = cpu_threads()
+    pos, vel, mass = I.uniform_ball(PP_N, seed=12345)
+    t1 = cpu_pp_step_seconds(pos, vel, mass, 1, threads)
+    steps = max(1, min(100, int(budget_s / max(t1, 1e-3))))
+    secs = cpu_pp_step_seconds(pos, vel, mass, steps, threads)
+    return {"value": float(PP_N) * PP_N * steps / secs, "unit": "interactions/s", "cores": threads,
+            "kind": cpu_kind(), "sample": f"{steps} full steps of the N=16384 workload (-v 2 OpenMP, "
+                                          f"{threads} threads)"}
+
+
+def bench_reference(args, world, rank):
+    if rank != 0:
+        return None
+    import pyoracle
+    from nbody_gb300 import initializers as I
+
+    pyoracle.build(reference=False)
+    threads = cpu_threads()
+    pos, vel, mass = I.uniform_ball(PP_N, seed=12345)
+    for _ in range(args.warmup):
+        cpu_pp_step_seconds(pos, vel, mass, 1, threads)
+    # each step is one full -v 2 step; the count is bounded to keep the run within minutes
+    t1 = cpu_pp_step_seconds(pos, vel, mass, 1, threads)
+    steps = max(1, min(args.steps, int(120.0 / max(t1, 1e-3))))
+    secs = cpu_pp_step_seconds(pos, vel, mass, steps, threads)
+    value = float(PP_N) * PP_N * steps / secs
+    kind = cpu_kind()
+    return {"impl": "reference", "metric": METRIC, "component": "PP interactions/s", "value": value,
+            "unit": "interactions/s", "n_gpus": world, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": secs * 1e3 / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "direct-sum PP, N=16384 uniform ball R=100, m~U[1,10), v=0, dt=0.0035, "
+                                   "eps2=40 (reference -v 2 path)", "n_bodies": PP_N, "parallelism": "host cores"},
+            "cpu_baseline": {"value": value, "unit": "interactions/s", "cores": threads, "kind": kind,
+                             "sample": f"{steps} full steps (-v 2 OpenMP, {threads} threads)"},
+            "e2e": {"value": value, "unit": "interactions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--workload", choices=["pp"], default="pp")
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        line = bench_reference(args, world, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    import nbody_gb300
+    from nbody_gb300 import build as nbuild
+
+    if not os.path.exists(nbody_gb300.LIB_PATH):
+        nbuild.build()
+    dist = init_dist(world, local)
+    line = bench_pp(args, world, rank, local, dist)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,123 @@
+/* nbody_gb300 — C ABI of the GB300-native (sm_103a) gravity solve.
+ *
+ * This is the drop-in boundary for the reference's solver plugin interface,
+ * MarcVivas/N-body `class ParticleSolver` (include/ParticleSolver.h:8-15):
+ *   updateParticlePositions(ParticleSystem*)   -> nbody_update_host
+ *   getSquaredSoftening()                       -> nbody_get_squared_softening
+ *   usesGPU()                                   -> (host arrays stay valid after
+ *                                                   every call: the adapter in
+ *                                                   ParticleSolverCUDA.h returns false)
+ * and for the solver constructors it replaces:
+ *   ParticleSolverCPUParallel(float timeStep, float squaredSoftening)
+ *     (include/ParticleSolverCPUParallel.h:9, -v 2; GPU form -v 3/-v 4,
+ *      include/ParticleSolverGPU.h)                    -> nbody_create(.., NBODY_MODE_PP, ..)
+ *   ParticleSolverBHutCPUParallel(float timeStep, float squaredSoftening, int n)
+ *     (include/ParticleSolverBHutCPUParallel.h:9, -v 6; GPU form -v 7)
+ *                                                       -> nbody_create(.., NBODY_MODE_BH, ..)
+ *
+ * Plain pointers and sizes only. Every entry point returns an int status
+ * (NBODY_OK or an NBODY_ERR_* code); no exception crosses this boundary. A
+ * context is not re-entrant: calls on one context must not overlap.
+ *
+ * Host arrays use the reference's ParticleSystem layout
+ * (include/ParticleSystem.h:100-104): float[4*n] per quantity, one (x,y,z,w)
+ * vec4 per body; positions carry w = 0 and masses live in masses4[4*i].
+ * Device-resident state uses this library's layout: pos_mass float4
+ * (x, y, z, m), vel float4 (x, y, z, 0), acc float4 (x, y, z, 0).
+ */
+#ifndef NBODY_GB300_H
+#define NBODY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NBODY_OK 0
+#define NBODY_ERR_ARG 1      /* bad argument (null pointer, n <= 0, unknown mode, ...) */
+#define NBODY_ERR_CUDA 2     /* a CUDA runtime call failed (see nbody_last_error)      */
+#define NBODY_ERR_NOMEM 3    /* device or pinned allocation failed                     */
+#define NBODY_ERR_CAPACITY 4 /* a fixed-size device structure would overflow           */
+#define NBODY_ERR_TIMEOUT 5  /* a bounded device-side wait gave up                     */
+#define NBODY_ERR_STATE 6    /* call out of order (e.g. step before upload)            */
+
+#define NBODY_MODE_PP 0 /* direct sum, reference -v 2 (CPU) / -v 3, -v 4 (GLSL)   */
+#define NBODY_MODE_BH 1 /* Barnes-Hut, reference -v 6 (CPU) / -v 7 (GLSL)         */
+
+typedef struct nbody_ctx nbody_ctx;
+
+/* Human-readable name of a status code. */
+const char *nbody_status_string(int status);
+
+/* Text of the last CUDA error seen by this context ("" if none). */
+const char *nbody_last_error(const nbody_ctx *ctx);
+
+/* Creates a solver for n bodies on CUDA device `device`: time step dt,
+ * squared softening eps2 (>= 0), theta2 = squared opening angle for BH
+ * (<= 0 selects the reference's 0.25, src/Octree/Octree.cpp:15; ignored for PP).
+ * G = 1 as in the reference (ParticleSolverCPUParallel.cpp:9). */
+int nbody_create(nbody_ctx **out, int device, int mode, int64_t n, float dt, float eps2, float theta2);
+int nbody_destroy(nbody_ctx *ctx);
+
+/* Launch work on `stream` (a cudaStream_t); NULL restores the context's own stream. */
+int nbody_set_stream(nbody_ctx *ctx, void *stream);
+
+/* ParticleSolver::getSquaredSoftening (include/ParticleSolver.h:13). */
+float nbody_get_squared_softening(const nbody_ctx *ctx);
+
+/* ParticleSolver::updateParticlePositions (include/ParticleSolver.h:12),
+ * repeated `steps` times, on host arrays in the ParticleSystem layout: copies
+ * positions, velocities, accelerations and masses in, advances, and copies
+ * positions, velocities, accelerations (and forces4, which may be NULL) back
+ * before returning. forces4 receives the acceleration evaluated at the
+ * positions the last step started from, as the reference's forces[] array.
+ * Pinned host memory makes the copies asynchronous DMA; pageable memory works. */
+int nbody_update_host(nbody_ctx *ctx, float *positions4, float *velocities4, float *accelerations4,
+                      const float *masses4, float *forces4, int steps);
+
+/* Resident mode: state stays in HBM between calls. */
+int nbody_upload(nbody_ctx *ctx, const float *positions4, const float *velocities4,
+                 const float *accelerations4, const float *masses4);
+int nbody_step(nbody_ctx *ctx, int steps);
+int nbody_download(nbody_ctx *ctx, float *positions4, float *velocities4, float *accelerations4,
+                   float *forces4);
+/* Waits for the context's stream and returns the device status word
+ * (NBODY_OK, or NBODY_ERR_TIMEOUT / NBODY_ERR_CAPACITY raised by a kernel). */
+int nbody_sync(nbody_ctx *ctx);
+
+/* Device pointers of the resident state (library layout, see above). */
+int nbody_device_state(nbody_ctx *ctx, void **pos_mass4, void **vel4, void **acc4);
+
+/* Direct-sum accelerations for n bodies on device buffers (library layout):
+ * force4[i] = sum_j m_j (x_j - x_i) / (|x_j - x_i|^2 + eps2)^1.5, the -v 2
+ * force (ParticleSolverCPUParallel.cpp:27-40). Runs on the context's stream,
+ * using the context's eps2 and its scratch memory. */
+int nbody_pp_forces_device(nbody_ctx *ctx, const void *pos_mass4, void *force4, int64_t n);
+
+/* One direct-sum step on device buffers: forces at pos_in, then the
+ * reference integrator (include/ParticleSystem.h:52-69) writing pos_out
+ * (pos_in != pos_out), vel4 and acc4 in place; force4 may be NULL. */
+int nbody_pp_step_device(nbody_ctx *ctx, const void *pos_in, void *pos_out, void *vel4, void *acc4,
+                         void *force4, int64_t n);
+
+/* Launch shape the direct-sum kernel picked for n bodies: i-bodies per
+ * thread, j-slices and CTAs. For tests and tuning reports. */
+int nbody_pp_config(nbody_ctx *ctx, int64_t n, int *bodies_per_thread, int *slices, int *ctas);
+
+/* Per-stage timing. While enabled, every kernel stage launched by this
+ * context is bracketed by a CUDA event pair on its launch stream.
+ * nbody_profile_read waits for them, writes the summed milliseconds and launch
+ * counts of stages 0..nstages-1, and clears the record. Stage names come from
+ * nbody_stage_name(0 .. nbody_stage_count()-1). */
+int nbody_profile_enable(nbody_ctx *ctx, int on);
+int nbody_profile_read(nbody_ctx *ctx, double *ms, int *launches, int nstages);
+const char *nbody_stage_name(int stage);
+int nbody_stage_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBODY_GB300_H */

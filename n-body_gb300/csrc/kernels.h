@@ -1,0 +1,50 @@
+// Host-side declarations of the kernel launchers (internal to the library).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nbody {
+
+// Reference-order integrator outputs (include/ParticleSystem.h:52-69).
+// pos_out == nullptr means "forces only".
+struct Integrate {
+    float4 *pos_out = nullptr;
+    float4 *vel = nullptr;
+    float4 *acc = nullptr;
+    float4 *force = nullptr;  // optional copy of the new acceleration
+    float dt = 0.f;
+};
+
+// Optional per-stage timing: when set, launchers record a CUDA event pair
+// around each kernel on the launch stream (see capi.cu: nbody_profile_*).
+enum Stage { kStagePPForce = 0, kStagePPReduce, kStagePack, kStageCount };
+
+struct StageTimer {
+    virtual ~StageTimer() = default;
+    virtual void begin(int stage, cudaStream_t s) = 0;
+    virtual void end(int stage, cudaStream_t s) = 0;
+};
+
+// Launch shape of the direct-sum force kernel for one n.
+struct PPPlan {
+    int k = 4;          // i-bodies per thread
+    int slices = 1;     // j-slices (CTAs per i-block)
+    int iblocks = 0;    // i-blocks of 128*k bodies
+    size_t partial_bytes = 0;  // scratch for per-slice partial accelerations
+};
+
+PPPlan pp_plan(int64_t n, int device);
+
+// Direct-sum forces at `pos` (float4 x,y,z,m) followed by the integrator
+// (or a plain force write when g.pos_out is null). `scratch` must hold
+// plan.partial_bytes when plan.slices > 1. `status` is a device int.
+cudaError_t pp_launch(const PPPlan &plan, const float4 *pos, int64_t n, float eps2, const Integrate &g,
+                      void *scratch, cudaStream_t stream, int *status, StageTimer *timer = nullptr);
+
+// Packs the reference host layout into the device layout and back.
+cudaError_t pack_state(const float4 *positions4, const float4 *masses4, float4 *pos_mass, int64_t n,
+                       cudaStream_t stream);
+cudaError_t unpack_positions(const float4 *pos_mass, float4 *positions4, int64_t n, cudaStream_t stream);
+
+}  // namespace nbody

@@ -1,0 +1,356 @@
+// Direct-sum (particle-particle) gravity for sm_103a.
+//
+// Replaces the reference's PP solvers: the CPU -v 2 force loop
+// (src/ParticleSolver/ParticleSolverCPUParallel/ParticleSolverCPUParallel.cpp:27-40)
+// and the GLSL -v 3 / -v 4 shaders (forceCalculation.glsl:24-49,
+// forceCalculationOptimized.glsl:28-76) plus the integrator, which here keeps
+// the CPU order (include/ParticleSystem.h:52-69), not the shaders' Euler step.
+//
+// Shape of the work: every CTA owns an i-block of 128*K bodies (K per thread,
+// held in registers) and one j-slice. The j-slice streams through shared
+// memory in tiles of 256 float4 (x, y, z, m) bodies, each fetched by one
+// non-tensor TMA bulk copy into a 3-stage ring completed on mbarriers. The
+// inner loop takes two j-bodies at a time so that every FP32 instruction is a
+// packed f32x2 one (FADD2/FFMA2/FMUL2): 12 packed ops + 2 MUFU.RSQ per pair of
+// interactions. j-slices exist to fill 152 SMs when n is small; their partial
+// accelerations are summed in slice order by a second kernel (deterministic)
+// which also applies the integrator. With one slice the integrator runs in the
+// force kernel's epilogue.
+//
+// Self-interaction: the reference skips j == i by index. Here the i == j term
+// has dx = 0 and contributes exactly 0 when eps2 > 0; with eps2 == 0 the GUARD
+// variant drops every pair at zero distance (r^2 == 0), which for j == i is the
+// same thing.
+#include <algorithm>
+#include <cstdlib>
+#include <mutex>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace nbody {
+
+constexpr int kPPThreads = 128;
+constexpr int kPPTile = 256;    // j-bodies per stage (4 KiB)
+constexpr int kPPStages = 3;
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+// Reference integrator, one body. Each operation is rounded on its own
+// (no FMA contraction), matching the reference's scalar evaluation.
+__device__ __forceinline__ void integrate_body(int64_t i, float4 p, float fx, float fy, float fz,
+                                               const Integrate &g) {
+    const float dt = g.dt;
+    const float h = __fmul_rn(dt, 0.5f);
+    float4 v = g.vel[i];
+    const float4 a = g.acc[i];
+    v.x = __fadd_rn(v.x, __fmul_rn(a.x, h));
+    v.y = __fadd_rn(v.y, __fmul_rn(a.y, h));
+    v.z = __fadd_rn(v.z, __fmul_rn(a.z, h));
+    p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
+    p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+    p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
+    v.x = __fadd_rn(v.x, __fmul_rn(fx, h));
+    v.y = __fadd_rn(v.y, __fmul_rn(fy, h));
+    v.z = __fadd_rn(v.z, __fmul_rn(fz, h));
+    const float4 anew = make_float4(fx, fy, fz, 0.f);
+    g.pos_out[i] = p;  // w keeps the mass
+    g.vel[i] = v;
+    g.acc[i] = anew;
+    if (g.force) g.force[i] = anew;
+}
+
+template <int K, bool GUARD>
+__global__ void __launch_bounds__(kPPThreads)
+    pp_force_kernel(const float4 *__restrict__ pos, int64_t n, float eps2, int nslices,
+                    float4 *__restrict__ partial, Integrate g, int *status) {
+    __shared__ __align__(128) float4 tile[kPPStages][kPPTile];
+    __shared__ __align__(8) uint64_t full[kPPStages];
+
+    const int tid = threadIdx.x;
+    const int64_t ib0 = static_cast<int64_t>(blockIdx.x) * (kPPThreads * K);
+    const int slice = blockIdx.y;
+    // The slice boundaries sit on even bodies so that j-pairs never straddle.
+    const int64_t npairs = (n + 1) / 2;
+    const int64_t p0 = npairs * slice / nslices;
+    const int64_t p1 = npairs * (slice + 1) / nslices;
+    const int64_t j0 = 2 * p0;
+    const int64_t j1 = (2 * p1 < n) ? 2 * p1 : n;
+    const int64_t len = j1 > j0 ? j1 - j0 : 0;
+    const int ntiles = static_cast<int>((len + kPPTile - 1) / kPPTile);
+
+    float2 nx[K], ny[K], nz[K], ax[K], ay[K], az[K];
+    float4 pi[K];
+#pragma unroll
+    for (int r = 0; r < K; ++r) {
+        const int64_t i = ib0 + tid + r * kPPThreads;
+        pi[r] = i < n ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        nx[r] = f2(-pi[r].x, -pi[r].x);
+        ny[r] = f2(-pi[r].y, -pi[r].y);
+        nz[r] = f2(-pi[r].z, -pi[r].z);
+        ax[r] = ay[r] = az[r] = f2(0.f, 0.f);
+    }
+    const float2 e2 = f2(eps2, eps2);
+
+    if (tid == 0) {
+        for (int s = 0; s < kPPStages; ++s) mbar_init(&full[s], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+
+    // Producer: thread 0 fetches tile t of this slice into stage t % kPPStages.
+    auto issue = [&](int t) {
+        const int stage = t % kPPStages;
+        const int64_t jt = j0 + static_cast<int64_t>(t) * kPPTile;
+        const int cnt = static_cast<int>((j1 - jt) < kPPTile ? (j1 - jt) : kPPTile);
+        if (cnt & 1) tile[stage][cnt] = make_float4(0.f, 0.f, 0.f, 0.f);  // pad the last pair: m = 0
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&full[stage], static_cast<uint32_t>(cnt) * 16u);
+        tma_bulk_g2s(&tile[stage][0], pos + jt, static_cast<uint32_t>(cnt) * 16u, &full[stage]);
+    };
+    if (tid == 0) {
+        for (int t = 0; t < kPPStages && t < ntiles; ++t) issue(t);
+    }
+
+    bool failed = false;
+    int t = 0;
+    for (; t < ntiles; ++t) {
+        const int stage = t % kPPStages;
+        const uint32_t parity = static_cast<uint32_t>(t / kPPStages) & 1u;
+        const bool ok = mbar_wait_bounded(&full[stage], parity, status);
+        if (!__syncthreads_and(ok)) {
+            failed = true;
+            break;
+        }
+        const int64_t jt = j0 + static_cast<int64_t>(t) * kPPTile;
+        const int cnt = static_cast<int>((j1 - jt) < kPPTile ? (j1 - jt) : kPPTile);
+        const int cnt2 = (cnt + 1) & ~1;
+        const float4 *tl = tile[stage];
+#pragma unroll 2
+        for (int jj = 0; jj < cnt2; jj += 2) {
+            const float4 a = tl[jj];
+            const float4 b = tl[jj + 1];
+            const float2 xj = f2(a.x, b.x), yj = f2(a.y, b.y), zj = f2(a.z, b.z), mj = f2(a.w, b.w);
+#pragma unroll
+            for (int r = 0; r < K; ++r) {
+                const float2 dx = __fadd2_rn(xj, nx[r]);
+                const float2 dy = __fadd2_rn(yj, ny[r]);
+                const float2 dz = __fadd2_rn(zj, nz[r]);
+                float2 r2 = __ffma2_rn(dx, dx, e2);
+                r2 = __ffma2_rn(dy, dy, r2);
+                r2 = __ffma2_rn(dz, dz, r2);
+                float2 inv = f2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+                if (GUARD) {
+                    inv.x = r2.x > 0.f ? inv.x : 0.f;
+                    inv.y = r2.y > 0.f ? inv.y : 0.f;
+                }
+                const float2 inv2 = __fmul2_rn(inv, inv);
+                const float2 s = __fmul2_rn(__fmul2_rn(mj, inv), inv2);
+                ax[r] = __ffma2_rn(dx, s, ax[r]);
+                ay[r] = __ffma2_rn(dy, s, ay[r]);
+                az[r] = __ffma2_rn(dz, s, az[r]);
+            }
+        }
+        __syncthreads();  // every thread is done with this stage
+        if (tid == 0 && t + kPPStages < ntiles) issue(t + kPPStages);
+    }
+
+    if (failed) {
+        // Drain this CTA's copies still in flight before shared memory goes away.
+        if (tid == 0) {
+            for (int u = t; u < ntiles && u < t + kPPStages; ++u)
+                mbar_wait_bounded(&full[u % kPPStages], static_cast<uint32_t>(u / kPPStages) & 1u, status);
+        }
+        __syncthreads();
+        return;
+    }
+
+#pragma unroll
+    for (int r = 0; r < K; ++r) {
+        const int64_t i = ib0 + tid + r * kPPThreads;
+        if (i >= n) continue;
+        const float fx = ax[r].x + ax[r].y;
+        const float fy = ay[r].x + ay[r].y;
+        const float fz = az[r].x + az[r].y;
+        if (partial) {
+            partial[static_cast<int64_t>(slice) * n + i] = make_float4(fx, fy, fz, 0.f);
+        } else if (g.pos_out) {
+            integrate_body(i, pi[r], fx, fy, fz, g);
+        } else if (g.force) {
+            g.force[i] = make_float4(fx, fy, fz, 0.f);
+        }
+    }
+}
+
+// Sums the per-slice partial accelerations in slice order, then integrates
+// (or writes forces only).
+__global__ void pp_reduce_kernel(const float4 *__restrict__ partial, int nslices, const float4 *__restrict__ pos,
+                                 int64_t n, Integrate g) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    for (int s = 0; s < nslices; ++s) {
+        const float4 q = partial[static_cast<int64_t>(s) * n + i];
+        fx += q.x;
+        fy += q.y;
+        fz += q.z;
+    }
+    if (g.pos_out) {
+        integrate_body(i, pos[i], fx, fy, fz, g);
+    } else if (g.force) {
+        g.force[i] = make_float4(fx, fy, fz, 0.f);
+    }
+}
+
+__global__ void pack_kernel(const float4 *__restrict__ positions4, const float4 *__restrict__ masses4,
+                            float4 *__restrict__ pos_mass, int64_t n) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = positions4[i];
+    pos_mass[i] = make_float4(p.x, p.y, p.z, masses4[i].x);
+}
+
+__global__ void unpack_kernel(const float4 *__restrict__ pos_mass, float4 *__restrict__ positions4, int64_t n) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos_mass[i];
+    positions4[i] = make_float4(p.x, p.y, p.z, 0.f);
+}
+
+// ---------------------------------------------------------------- host side
+namespace {
+
+template <int K>
+int ctas_per_sm() {
+    int c = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, pp_force_kernel<K, false>, kPPThreads, 0);
+    return c > 0 ? c : 1;
+}
+
+struct DeviceInfo {
+    int sms = 0;
+    int cps[4] = {0, 0, 0, 0};  // CTAs per SM for K = 1, 2, 4, 8
+};
+
+DeviceInfo device_info(int device) {
+    static std::mutex mu;
+    static DeviceInfo cache[64];
+    static bool have[64] = {};
+    std::lock_guard<std::mutex> lk(mu);
+    if (device < 0 || device >= 64) device = 0;
+    if (!have[device]) {
+        DeviceInfo d;
+        cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, device);
+        d.cps[0] = ctas_per_sm<1>();
+        d.cps[1] = ctas_per_sm<2>();
+        d.cps[2] = ctas_per_sm<4>();
+        d.cps[3] = ctas_per_sm<8>();
+        cache[device] = d;
+        have[device] = true;
+    }
+    return cache[device];
+}
+
+int k_index(int k) { return k == 1 ? 0 : k == 2 ? 1 : k == 4 ? 2 : 3; }
+
+}  // namespace
+
+PPPlan pp_plan(int64_t n, int device) {
+    PPPlan p;
+    const DeviceInfo d = device_info(device);
+    int k = 4;
+    if (const char *e = std::getenv("NBODY_PP_K")) {
+        const int v = std::atoi(e);
+        if (v == 1 || v == 2 || v == 4 || v == 8) k = v;
+    } else if (n <= 2 * kPPThreads) {
+        k = 1;
+    }
+    p.k = k;
+    const int64_t per_block = static_cast<int64_t>(kPPThreads) * k;
+    p.iblocks = static_cast<int>((n + per_block - 1) / per_block);
+    const int sms = d.sms > 0 ? d.sms : 1;
+    const int64_t slots = static_cast<int64_t>(sms) * d.cps[k_index(k)];
+    const int64_t npairs = (n + 1) / 2;
+    // Each slice keeps at least one full tile of j-bodies.
+    int64_t smax = npairs / (kPPTile / 2);
+    smax = std::max<int64_t>(1, std::min<int64_t>(smax, 64));
+    if (const char *e = std::getenv("NBODY_PP_SLICES")) {
+        const int v = std::atoi(e);
+        if (v >= 1) smax = std::min<int64_t>(smax, v);
+    }
+    // Pick the slice count that best balances CTAs over SMs and fills the
+    // resident slots, with a small charge per extra slice for the partials.
+    double best = -1.0;
+    int best_s = 1;
+    for (int64_t s = 1; s <= smax; ++s) {
+        const int64_t total = static_cast<int64_t>(p.iblocks) * s;
+        const int64_t per_sm = (total + sms - 1) / sms;
+        const double eff = static_cast<double>(total) / static_cast<double>(per_sm * sms);
+        const double fill = std::min(1.0, static_cast<double>(total) / static_cast<double>(slots));
+        const double score = eff * fill / (1.0 + 0.01 * static_cast<double>(s));
+        if (score > best + 1e-12) {
+            best = score;
+            best_s = static_cast<int>(s);
+        }
+    }
+    if (const char *e = std::getenv("NBODY_PP_SLICES")) {
+        const int v = std::atoi(e);
+        if (v >= 1) best_s = static_cast<int>(std::min<int64_t>(v, std::max<int64_t>(1, npairs)));
+    }
+    p.slices = best_s;
+    p.partial_bytes = p.slices > 1 ? static_cast<size_t>(p.slices) * static_cast<size_t>(n) * sizeof(float4) : 0;
+    return p;
+}
+
+template <int K>
+static cudaError_t launch_k(const PPPlan &plan, const float4 *pos, int64_t n, float eps2, const Integrate &g,
+                            float4 *partial, cudaStream_t stream, int *status) {
+    const dim3 grid(plan.iblocks, plan.slices);
+    if (eps2 > 0.f)
+        pp_force_kernel<K, false><<<grid, kPPThreads, 0, stream>>>(pos, n, eps2, plan.slices, partial, g, status);
+    else
+        pp_force_kernel<K, true><<<grid, kPPThreads, 0, stream>>>(pos, n, eps2, plan.slices, partial, g, status);
+    return cudaGetLastError();
+}
+
+cudaError_t pp_launch(const PPPlan &plan, const float4 *pos, int64_t n, float eps2, const Integrate &g,
+                      void *scratch, cudaStream_t stream, int *status, StageTimer *timer) {
+    if (n <= 0) return cudaSuccess;
+    float4 *partial = plan.slices > 1 ? static_cast<float4 *>(scratch) : nullptr;
+    if (plan.slices > 1 && !partial) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if (timer) timer->begin(kStagePPForce, stream);
+    switch (plan.k) {
+        case 1: e = launch_k<1>(plan, pos, n, eps2, g, partial, stream, status); break;
+        case 2: e = launch_k<2>(plan, pos, n, eps2, g, partial, stream, status); break;
+        case 8: e = launch_k<8>(plan, pos, n, eps2, g, partial, stream, status); break;
+        default: e = launch_k<4>(plan, pos, n, eps2, g, partial, stream, status); break;
+    }
+    if (timer) timer->end(kStagePPForce, stream);
+    if (e != cudaSuccess || plan.slices <= 1) return e;
+    const int threads = 256;
+    const int64_t blocks = (n + threads - 1) / threads;
+    if (timer) timer->begin(kStagePPReduce, stream);
+    pp_reduce_kernel<<<static_cast<unsigned>(blocks), threads, 0, stream>>>(partial, plan.slices, pos, n, g);
+    if (timer) timer->end(kStagePPReduce, stream);
+    return cudaGetLastError();
+}
+
+cudaError_t pack_state(const float4 *positions4, const float4 *masses4, float4 *pos_mass, int64_t n,
+                       cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    pack_kernel<<<static_cast<unsigned>((n + threads - 1) / threads), threads, 0, stream>>>(positions4, masses4,
+                                                                                           pos_mass, n);
+    return cudaGetLastError();
+}
+
+cudaError_t unpack_positions(const float4 *pos_mass, float4 *positions4, int64_t n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    unpack_kernel<<<static_cast<unsigned>((n + threads - 1) / threads), threads, 0, stream>>>(pos_mass,
+                                                                                             positions4, n);
+    return cudaGetLastError();
+}
+
+}  // namespace nbody

@@ -1,0 +1,191 @@
+"""Direct-sum (PP) CUDA path vs the oracle: the reference's own -v 2 outputs
+(golden fixtures), the C restatement, and an FP64 direct sum.
+
+Tolerances (FP32 throughout; the kernel uses the hardware rsqrt and FMA where
+the reference uses pow(x, 1.5) and a divide):
+  * accelerations: per-body relative error RMS <= 1e-5, max <= 1e-3
+    (the max allows for bodies whose net force nearly cancels);
+  * vs FP64 at the 16,384-body ball: RMS <= 1e-5 (the accuracy gate);
+  * positions / velocities after k steps: rtol 1e-5 against the reference.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden, rel_err_stats
+
+pytestmark = pytest.mark.gpu
+
+PP_FIXTURES = ["pp_ball_1024.npz", "pp_ball_1000.npz", "pp_small_1.npz", "pp_small_2.npz", "pp_small_3.npz",
+               "pp_small_5.npz", "pp_small_127.npz", "pp_eps0_64.npz"]
+
+
+def run_host(nb, g, steps):
+    n = len(g["mass"])
+    sysm = nb.ParticleSystem(g["pos"].copy(), g["vel"].copy(), g["mass"], g["acc"].copy())
+    solver = nb.ParticleSolverCUDA(float(g["dt"]), float(g["eps2"]), n, mode="pp")
+    solver.update_particle_positions(sysm, steps=steps)
+    solver.close()
+    return sysm
+
+
+def check_forces(got, ref, rms_tol=1e-5, max_tol=1e-3):
+    if np.abs(ref[:, :3]).max() == 0:
+        assert np.abs(got[:, :3]).max() == 0
+        return
+    rms, mx = rel_err_stats(got, ref)
+    assert rms <= rms_tol and mx <= max_tol, (rms, mx)
+
+
+@pytest.mark.parametrize("name", PP_FIXTURES)
+def test_pp_matches_reference_golden(nb, cuda, name):
+    g = golden(name)
+    s1 = run_host(nb, g, 1)
+    check_forces(s1.forces, g["force1"])
+    check_forces(s1.accelerations, g["acc1"])
+    np.testing.assert_allclose(s1.positions, g["pos1"], rtol=1e-6, atol=1e-6)
+    sk = run_host(nb, g, int(g["steps"]))
+    check_forces(sk.forces, g["forcek"])
+    np.testing.assert_allclose(sk.positions, g["posk"], rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(sk.velocities, g["velk"], rtol=1e-5, atol=1e-5)
+    assert np.all(sk.positions[:, 3] == 0)  # reference layout: w = 0
+
+
+def test_pp_lagrange_1000_steps(nb, cuda):
+    g = golden("lagrange.npz")
+    s = run_host(nb, g, int(g["steps"]))
+    np.testing.assert_allclose(s.positions, g["posk"], rtol=1e-4, atol=1e-4)
+    np.testing.assert_allclose(s.velocities, g["velk"], rtol=1e-3, atol=1e-3)
+
+
+def test_pp_config1_accuracy_vs_fp64_and_port(nb, cuda, oracle):
+    from nbody_gb300 import initializers as I
+
+    n = 16384
+    pos, vel, mass = I.uniform_ball(n, seed=12345)
+    sysm = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+    solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp")
+    solver.update_particle_positions(sysm)
+    a64 = oracle.direct_f64(pos, mass, 40.0)
+    rms, mx = rel_err_stats(sysm.forces, a64)
+    assert rms <= 1e-5, (rms, mx)
+    f32 = oracle.pp_forces(pos, mass, 40.0)
+    check_forces(sysm.forces, f32)
+    # Newton's third law: total momentum change ~ 0
+    p = (mass[:, None] * sysm.forces[:, :3].astype(np.float64)).sum(0)
+    scale = (mass[:, None] * np.abs(sysm.forces[:, :3].astype(np.float64))).sum()
+    assert np.abs(p).max() < 1e-5 * scale
+
+
+def test_pp_config1_ten_steps_vs_port(nb, cuda, oracle):
+    from nbody_gb300 import initializers as I
+
+    n = 16384
+    pos, vel, mass = I.uniform_ball(n, seed=12345)
+    acc = np.zeros_like(pos)
+    sysm = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+    nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp").update_particle_positions(sysm, steps=10)
+    pk, vk, ak, fk, _ = oracle.pp_run(pos, vel, acc, mass, 0.0035, 40.0, 10)
+    check_forces(sysm.forces, fk)
+    np.testing.assert_allclose(sysm.positions, pk, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(sysm.velocities, vk, rtol=1e-4, atol=1e-6)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 255, 256, 257, 511, 513, 1000, 4097, 33333])
+def test_pp_ragged_sizes_vs_port(nb, cuda, oracle, n):
+    from nbody_gb300 import initializers as I
+
+    pos, vel, mass = I.uniform_ball(n, seed=n)
+    sysm = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+    nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp").update_particle_positions(sysm)
+    check_forces(sysm.forces, oracle.pp_forces(pos, mass, 40.0))
+
+
+def test_pp_slicing_does_not_change_forces(nb, cuda, monkeypatch):
+    from nbody_gb300 import initializers as I
+
+    n = 8192
+    pos, vel, mass = I.uniform_ball(n, seed=3)
+    out = {}
+    for s in ("1", "7", "32"):
+        monkeypatch.setenv("NBODY_PP_SLICES", s)
+        solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp")
+        assert solver.pp_config()["slices"] == int(s)
+        sysm = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+        solver.update_particle_positions(sysm)
+        out[s] = sysm.forces.copy()
+    check_forces(out["7"], out["1"], rms_tol=1e-6, max_tol=1e-4)
+    check_forces(out["32"], out["1"], rms_tol=1e-6, max_tol=1e-4)
+
+
+@pytest.mark.parametrize("k", ["1", "2", "4", "8"])
+def test_pp_bodies_per_thread_variants(nb, cuda, oracle, monkeypatch, k):
+    from nbody_gb300 import initializers as I
+
+    monkeypatch.setenv("NBODY_PP_K", k)
+    n = 3000
+    pos, vel, mass = I.uniform_ball(n, seed=4)
+    solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp")
+    assert solver.pp_config()["bodies_per_thread"] == int(k)
+    sysm = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+    solver.update_particle_positions(sysm)
+    check_forces(sysm.forces, oracle.pp_forces(pos, mass, 40.0))
+
+
+def test_pp_device_entry_points_match_host_path(nb, cuda):
+    torch = cuda
+    from nbody_gb300 import initializers as I
+
+    n = 5000
+    pos, vel, mass = I.uniform_ball(n, seed=5)
+    acc = np.zeros_like(pos)
+    pm = torch.from_numpy(I.pos_mass(pos, mass)).cuda()
+    force = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp")
+    solver.set_stream(torch.cuda.current_stream().cuda_stream)
+    solver.pp_forces_device(pm, force)
+    torch.cuda.synchronize()
+    sysm = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+    solver.set_stream(None)
+    solver.update_particle_positions(sysm)
+    np.testing.assert_array_equal(force.cpu().numpy(), sysm.forces)
+    # one device step == one host step
+    solver.set_stream(torch.cuda.current_stream().cuda_stream)
+    pout = torch.empty_like(pm)
+    v = torch.from_numpy(vel.copy()).cuda()
+    a = torch.from_numpy(acc.copy()).cuda()
+    solver.pp_step_device(pm, pout, v, a)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(pout.cpu().numpy()[:, :3], sysm.positions[:, :3])
+    np.testing.assert_array_equal(v.cpu().numpy(), sysm.velocities)
+    np.testing.assert_array_equal(a.cpu().numpy(), sysm.accelerations)
+    assert np.all(pout.cpu().numpy()[:, 3] == mass)
+
+
+def test_pp_resident_mode_equals_host_calls_and_is_deterministic(nb, cuda):
+    from nbody_gb300 import initializers as I
+
+    n = 4096
+    pos, vel, mass = I.uniform_ball(n, seed=6)
+    a = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+    solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp")
+    for _ in range(5):
+        solver.update_particle_positions(a)
+    b = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+    solver.upload(b)
+    solver.step(5)
+    solver.download(b)
+    for x, y in ((a.positions, b.positions), (a.velocities, b.velocities), (a.accelerations, b.accelerations),
+                 (a.forces, b.forces)):
+        np.testing.assert_array_equal(x, y)
+    solver.sync()
+
+
+def test_pp_rejects_misaligned_device_pointer(nb, cuda):
+    torch = cuda
+    solver = nb.ParticleSolverCUDA(0.0035, 40.0, 64, mode="pp")
+    buf = torch.zeros(64 * 4 + 1, dtype=torch.float32, device="cuda")
+    with pytest.raises(nb.NBodyError) as e:
+        solver.pp_forces_device(buf.data_ptr() + 4, buf.data_ptr(), 64)
+    assert e.value.status == nb.ERR_ARG
