@@ -177,12 +177,15 @@ def bench_pp(args, world, rank, local, dist):
     pos, vel, mass = I.uniform_ball(n, seed=12345 + rank)
     system = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
     solver = nb.ParticleSolverCUDA(PP_DT, PP_EPS2, n, mode="pp", device=local)
-    stream = torch.cuda.current_stream()
+    # A dedicated (non-legacy) stream: the library launches on it and the
+    # CUDA events below are recorded on it.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     solver.set_stream(stream.cuda_stream)
     solver.upload(system)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     cfg = solver.pp_config()
-    launches_per_step = 1 + (1 if cfg["slices"] > 1 else 0)
+    launches_per_step = 1  # one pp_force_kernel launch per step (slices reduce inside it)
 
     def timed_steps(k, profile=False):
         evs = []

@@ -130,6 +130,7 @@ int ensure_scratch(nbody_ctx *ctx, size_t bytes) {
         ctx->scratch_bytes = 0;
     }
     NB_CK(ctx, cudaMalloc(&ctx->scratch, bytes));
+    NB_CK(ctx, cudaMemsetAsync(ctx->scratch, 0, bytes, ctx->stream));
     ctx->scratch_bytes = bytes;
     return NBODY_OK;
 }
@@ -139,6 +140,11 @@ int read_status(nbody_ctx *ctx) {
     NB_CK(ctx, cudaMemcpyAsync(&h, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     NB_CK(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream));
     NB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h != NBODY_OK && ctx->scratch) {
+        // A kernel gave up part-way: its arrival counters may be left non-zero.
+        NB_CK(ctx, cudaMemsetAsync(ctx->scratch, 0, ctx->scratch_bytes, ctx->stream));
+        NB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    }
     return h;
 }
 
@@ -367,7 +373,6 @@ int nbody_pp_config(nbody_ctx *ctx, int64_t n, int *bodies_per_thread, int *slic
 const char *nbody_stage_name(int stage) {
     switch (stage) {
         case nbody::kStagePPForce: return "pp_force";
-        case nbody::kStagePPReduce: return "pp_reduce_integrate";
         case nbody::kStagePack: return "pack";
         default: return "";
     }

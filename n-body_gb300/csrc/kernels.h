@@ -18,7 +18,7 @@ struct Integrate {
 
 // Optional per-stage timing: when set, launchers record a CUDA event pair
 // around each kernel on the launch stream (see capi.cu: nbody_profile_*).
-enum Stage { kStagePPForce = 0, kStagePPReduce, kStagePack, kStageCount };
+enum Stage { kStagePPForce = 0, kStagePack, kStageCount };
 
 struct StageTimer {
     virtual ~StageTimer() = default;
@@ -31,14 +31,17 @@ struct PPPlan {
     int k = 4;          // i-bodies per thread
     int slices = 1;     // j-slices (CTAs per i-block)
     int iblocks = 0;    // i-blocks of 128*k bodies
-    size_t partial_bytes = 0;  // scratch for per-slice partial accelerations
+    size_t arrivals_bytes = 0; // per-i-block arrival counters at the start of scratch (zeroed once)
+    size_t partial_bytes = 0;  // total scratch: counters + per-slice partial accelerations
 };
 
 PPPlan pp_plan(int64_t n, int device);
 
 // Direct-sum forces at `pos` (float4 x,y,z,m) followed by the integrator
-// (or a plain force write when g.pos_out is null). `scratch` must hold
-// plan.partial_bytes when plan.slices > 1. `status` is a device int.
+// (or a plain force write when g.pos_out is null). When plan.slices > 1,
+// `scratch` must hold plan.partial_bytes and its first plan.arrivals_bytes
+// must be zero before the first launch (the kernel leaves them zero again).
+// `status` is a device int.
 cudaError_t pp_launch(const PPPlan &plan, const float4 *pos, int64_t n, float eps2, const Integrate &g,
                       void *scratch, cudaStream_t stream, int *status, StageTimer *timer = nullptr);
 

@@ -63,9 +63,10 @@ __device__ __forceinline__ void integrate_body(int64_t i, float4 p, float fx, fl
 template <int K, bool GUARD>
 __global__ void __launch_bounds__(kPPThreads)
     pp_force_kernel(const float4 *__restrict__ pos, int64_t n, float eps2, int nslices,
-                    float4 *__restrict__ partial, Integrate g, int *status) {
+                    float4 *__restrict__ partial, unsigned *__restrict__ arrivals, Integrate g, int *status) {
     __shared__ __align__(128) float4 tile[kPPStages][kPPTile];
     __shared__ __align__(8) uint64_t full[kPPStages];
+    __shared__ int last_cta;
 
     const int tid = threadIdx.x;
     const int64_t ib0 = static_cast<int64_t>(blockIdx.x) * (kPPThreads * K);
@@ -165,40 +166,61 @@ __global__ void __launch_bounds__(kPPThreads)
         return;
     }
 
+    if (nslices == 1) {
+#pragma unroll
+        for (int r = 0; r < K; ++r) {
+            const int64_t i = ib0 + tid + r * kPPThreads;
+            if (i >= n) continue;
+            const float fx = ax[r].x + ax[r].y;
+            const float fy = ay[r].x + ay[r].y;
+            const float fz = az[r].x + az[r].y;
+            if (g.pos_out) integrate_body(i, pi[r], fx, fy, fz, g);
+            else if (g.force) g.force[i] = make_float4(fx, fy, fz, 0.f);
+        }
+        return;
+    }
+
+    // Several j-slices: publish this slice's partial accelerations; the CTA
+    // that completes an i-block last sums all slices in slice order (so the
+    // result does not depend on which CTA ran when) and integrates.
+#pragma unroll
+    for (int r = 0; r < K; ++r) {
+        const int64_t i = ib0 + tid + r * kPPThreads;
+        if (i < n)
+            partial[static_cast<int64_t>(slice) * n + i] =
+                make_float4(ax[r].x + ax[r].y, ay[r].x + ay[r].y, az[r].x + az[r].y, 0.f);
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned prev = atomicAdd(&arrivals[blockIdx.x], 1u);
+        last_cta = (prev == static_cast<unsigned>(nslices - 1));
+        if (last_cta) arrivals[blockIdx.x] = 0u;  // ready for the next launch
+    }
+    __syncthreads();
+    if (!last_cta) return;
+    __threadfence();
+    float fx[K], fy[K], fz[K];
+#pragma unroll
+    for (int r = 0; r < K; ++r) fx[r] = fy[r] = fz[r] = 0.f;
+    for (int sl = 0; sl < nslices; ++sl) {
+#pragma unroll
+        for (int r = 0; r < K; ++r) {
+            const int64_t i = ib0 + tid + r * kPPThreads;
+            if (i < n) {
+                const float4 q = __ldcg(&partial[static_cast<int64_t>(sl) * n + i]);
+                fx[r] += q.x;
+                fy[r] += q.y;
+                fz[r] += q.z;
+            }
+        }
+    }
 #pragma unroll
     for (int r = 0; r < K; ++r) {
         const int64_t i = ib0 + tid + r * kPPThreads;
         if (i >= n) continue;
-        const float fx = ax[r].x + ax[r].y;
-        const float fy = ay[r].x + ay[r].y;
-        const float fz = az[r].x + az[r].y;
-        if (partial) {
-            partial[static_cast<int64_t>(slice) * n + i] = make_float4(fx, fy, fz, 0.f);
-        } else if (g.pos_out) {
-            integrate_body(i, pi[r], fx, fy, fz, g);
-        } else if (g.force) {
-            g.force[i] = make_float4(fx, fy, fz, 0.f);
-        }
-    }
-}
-
-// Sums the per-slice partial accelerations in slice order, then integrates
-// (or writes forces only).
-__global__ void pp_reduce_kernel(const float4 *__restrict__ partial, int nslices, const float4 *__restrict__ pos,
-                                 int64_t n, Integrate g) {
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float fx = 0.f, fy = 0.f, fz = 0.f;
-    for (int s = 0; s < nslices; ++s) {
-        const float4 q = partial[static_cast<int64_t>(s) * n + i];
-        fx += q.x;
-        fy += q.y;
-        fz += q.z;
-    }
-    if (g.pos_out) {
-        integrate_body(i, pos[i], fx, fy, fz, g);
-    } else if (g.force) {
-        g.force[i] = make_float4(fx, fy, fz, 0.f);
+        if (g.pos_out) integrate_body(i, pi[r], fx[r], fy[r], fz[r], g);
+        else if (g.force) g.force[i] = make_float4(fx[r], fy[r], fz[r], 0.f);
     }
 }
 
@@ -268,29 +290,26 @@ PPPlan pp_plan(int64_t n, int device) {
     p.k = k;
     const int64_t per_block = static_cast<int64_t>(kPPThreads) * k;
     p.iblocks = static_cast<int>((n + per_block - 1) / per_block);
-    const int sms = d.sms > 0 ? d.sms : 1;
-    const int64_t slots = static_cast<int64_t>(sms) * d.cps[k_index(k)];
+    const int64_t sms = d.sms > 0 ? d.sms : 1;
+    const int64_t cps = d.cps[k_index(k)] > 0 ? d.cps[k_index(k)] : 1;
     const int64_t npairs = (n + 1) / 2;
-    // Each slice keeps at least one full tile of j-bodies.
-    int64_t smax = npairs / (kPPTile / 2);
-    smax = std::max<int64_t>(1, std::min<int64_t>(smax, 64));
-    if (const char *e = std::getenv("NBODY_PP_SLICES")) {
-        const int v = std::atoi(e);
-        if (v >= 1) smax = std::min<int64_t>(smax, v);
-    }
-    // Pick the slice count that best balances CTAs over SMs and fills the
-    // resident slots, with a small charge per extra slice for the partials.
-    double best = -1.0;
+    // Slice count: each slice keeps at least one full tile of j-bodies. The
+    // cost model charges every SM for the waves of CTAs it must run (a partial
+    // wave costs a full one, since a lone CTA cannot fill an SM), each CTA for
+    // its j-pairs plus a fixed overhead (pipeline fill, i-loads, epilogue), and
+    // the final sum for reading one partial per slice.
+    int64_t smax = std::max<int64_t>(1, std::min<int64_t>(npairs / (kPPTile / 2), 64));
+    double best = 1e300;
     int best_s = 1;
-    for (int64_t s = 1; s <= smax; ++s) {
-        const int64_t total = static_cast<int64_t>(p.iblocks) * s;
+    for (int64_t sl = 1; sl <= smax; ++sl) {
+        const int64_t total = static_cast<int64_t>(p.iblocks) * sl;
         const int64_t per_sm = (total + sms - 1) / sms;
-        const double eff = static_cast<double>(total) / static_cast<double>(per_sm * sms);
-        const double fill = std::min(1.0, static_cast<double>(total) / static_cast<double>(slots));
-        const double score = eff * fill / (1.0 + 0.01 * static_cast<double>(s));
-        if (score > best + 1e-12) {
-            best = score;
-            best_s = static_cast<int>(s);
+        const int64_t waves = (per_sm + cps - 1) / cps;
+        const double cta_cost = static_cast<double>(npairs) / static_cast<double>(sl) + 128.0;
+        const double cost = static_cast<double>(waves * cps) * cta_cost + 8.0 * static_cast<double>(sl);
+        if (cost < best * (1.0 - 1e-9)) {
+            best = cost;
+            best_s = static_cast<int>(sl);
         }
     }
     if (const char *e = std::getenv("NBODY_PP_SLICES")) {
@@ -298,42 +317,46 @@ PPPlan pp_plan(int64_t n, int device) {
         if (v >= 1) best_s = static_cast<int>(std::min<int64_t>(v, std::max<int64_t>(1, npairs)));
     }
     p.slices = best_s;
-    p.partial_bytes = p.slices > 1 ? static_cast<size_t>(p.slices) * static_cast<size_t>(n) * sizeof(float4) : 0;
+    if (p.slices > 1) {
+        p.arrivals_bytes = (static_cast<size_t>(p.iblocks) * sizeof(unsigned) + 255) & ~static_cast<size_t>(255);
+        p.partial_bytes = p.arrivals_bytes + static_cast<size_t>(p.slices) * static_cast<size_t>(n) * sizeof(float4);
+    }
     return p;
 }
 
 template <int K>
 static cudaError_t launch_k(const PPPlan &plan, const float4 *pos, int64_t n, float eps2, const Integrate &g,
-                            float4 *partial, cudaStream_t stream, int *status) {
+                            float4 *partial, unsigned *arrivals, cudaStream_t stream, int *status) {
     const dim3 grid(plan.iblocks, plan.slices);
     if (eps2 > 0.f)
-        pp_force_kernel<K, false><<<grid, kPPThreads, 0, stream>>>(pos, n, eps2, plan.slices, partial, g, status);
+        pp_force_kernel<K, false><<<grid, kPPThreads, 0, stream>>>(pos, n, eps2, plan.slices, partial, arrivals, g,
+                                                                    status);
     else
-        pp_force_kernel<K, true><<<grid, kPPThreads, 0, stream>>>(pos, n, eps2, plan.slices, partial, g, status);
+        pp_force_kernel<K, true><<<grid, kPPThreads, 0, stream>>>(pos, n, eps2, plan.slices, partial, arrivals, g,
+                                                                   status);
     return cudaGetLastError();
 }
 
 cudaError_t pp_launch(const PPPlan &plan, const float4 *pos, int64_t n, float eps2, const Integrate &g,
                       void *scratch, cudaStream_t stream, int *status, StageTimer *timer) {
     if (n <= 0) return cudaSuccess;
-    float4 *partial = plan.slices > 1 ? static_cast<float4 *>(scratch) : nullptr;
-    if (plan.slices > 1 && !partial) return cudaErrorInvalidValue;
+    unsigned *arrivals = nullptr;
+    float4 *partial = nullptr;
+    if (plan.slices > 1) {
+        if (!scratch) return cudaErrorInvalidValue;
+        arrivals = static_cast<unsigned *>(scratch);
+        partial = reinterpret_cast<float4 *>(static_cast<char *>(scratch) + plan.arrivals_bytes);
+    }
     cudaError_t e;
     if (timer) timer->begin(kStagePPForce, stream);
     switch (plan.k) {
-        case 1: e = launch_k<1>(plan, pos, n, eps2, g, partial, stream, status); break;
-        case 2: e = launch_k<2>(plan, pos, n, eps2, g, partial, stream, status); break;
-        case 8: e = launch_k<8>(plan, pos, n, eps2, g, partial, stream, status); break;
-        default: e = launch_k<4>(plan, pos, n, eps2, g, partial, stream, status); break;
+        case 1: e = launch_k<1>(plan, pos, n, eps2, g, partial, arrivals, stream, status); break;
+        case 2: e = launch_k<2>(plan, pos, n, eps2, g, partial, arrivals, stream, status); break;
+        case 8: e = launch_k<8>(plan, pos, n, eps2, g, partial, arrivals, stream, status); break;
+        default: e = launch_k<4>(plan, pos, n, eps2, g, partial, arrivals, stream, status); break;
     }
     if (timer) timer->end(kStagePPForce, stream);
-    if (e != cudaSuccess || plan.slices <= 1) return e;
-    const int threads = 256;
-    const int64_t blocks = (n + threads - 1) / threads;
-    if (timer) timer->begin(kStagePPReduce, stream);
-    pp_reduce_kernel<<<static_cast<unsigned>(blocks), threads, 0, stream>>>(partial, plan.slices, pos, n, g);
-    if (timer) timer->end(kStagePPReduce, stream);
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t pack_state(const float4 *positions4, const float4 *masses4, float4 *pos_mass, int64_t n,
