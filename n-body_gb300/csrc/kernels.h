@@ -29,8 +29,9 @@ struct StageTimer {
 // Launch shape of the direct-sum force kernel for one n.
 struct PPPlan {
     int k = 4;          // i-bodies per thread
+    int threads = 128;  // threads per CTA
     int slices = 1;     // j-slices (CTAs per i-block)
-    int iblocks = 0;    // i-blocks of 128*k bodies
+    int iblocks = 0;    // i-blocks of threads*k bodies
     size_t arrivals_bytes = 0; // per-i-block arrival counters at the start of scratch (zeroed once)
     size_t partial_bytes = 0;  // total scratch: counters + per-slice partial accelerations
 };

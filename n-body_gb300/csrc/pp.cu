@@ -6,13 +6,13 @@
 // forceCalculationOptimized.glsl:28-76) plus the integrator, which here keeps
 // the CPU order (include/ParticleSystem.h:52-69), not the shaders' Euler step.
 //
-// Shape of the work: every CTA owns an i-block of 128*K bodies (K per thread,
+// Shape of the work: every CTA owns an i-block of T*K bodies (K per thread,
 // held in registers) and one j-slice. The j-slice streams through shared
 // memory in tiles of 256 float4 (x, y, z, m) bodies, each fetched by one
-// non-tensor TMA bulk copy into a 3-stage ring completed on mbarriers. The
-// inner loop takes two j-bodies at a time so that every FP32 instruction is a
-// packed f32x2 one (FADD2/FFMA2/FMUL2): 12 packed ops + 2 MUFU.RSQ per pair of
-// interactions. j-slices exist to fill 152 SMs when n is small; their partial
+// non-tensor TMA bulk copy into a 3-stage ring completed on mbarriers; each
+// landed tile is re-laid as j-pairs. The inner loop takes two j-bodies at a
+// time so that every FP32 instruction is a packed f32x2 one
+// (FADD2/FFMA2/FMUL2): 12 packed ops + 2 MUFU.RSQ per pair of interactions. j-slices exist to fill 152 SMs when n is small; their partial
 // accelerations are summed in slice order by a second kernel (deterministic)
 // which also applies the integrator. With one slice the integrator runs in the
 // force kernel's epilogue.
@@ -30,7 +30,7 @@
 
 namespace nbody {
 
-constexpr int kPPThreads = 128;
+constexpr int kPPMinThreads = 128;
 constexpr int kPPTile = 256;    // j-bodies per stage (4 KiB)
 constexpr int kPPStages = 3;
 
@@ -60,16 +60,20 @@ __device__ __forceinline__ void integrate_body(int64_t i, float4 p, float fx, fl
     if (g.force) g.force[i] = anew;
 }
 
-template <int K, bool GUARD>
-__global__ void __launch_bounds__(kPPThreads)
+template <int K, int T, bool GUARD>
+__global__ void __launch_bounds__(T)
     pp_force_kernel(const float4 *__restrict__ pos, int64_t n, float eps2, int nslices,
                     float4 *__restrict__ partial, unsigned *__restrict__ arrivals, Integrate g, int *status) {
+    // tile: TMA landing zone, bodies as float4 (x, y, z, m).
+    // pairs: the current tile re-laid as j-pairs {x0 x1 y0 y1}{z0 z1 m0 m1}, so
+    // that one 16-byte shared load yields two packed f32x2 operands.
     __shared__ __align__(128) float4 tile[kPPStages][kPPTile];
+    __shared__ __align__(128) float4 pairs[kPPTile];
     __shared__ __align__(8) uint64_t full[kPPStages];
     __shared__ int last_cta;
 
     const int tid = threadIdx.x;
-    const int64_t ib0 = static_cast<int64_t>(blockIdx.x) * (kPPThreads * K);
+    const int64_t ib0 = static_cast<int64_t>(blockIdx.x) * (T * K);
     const int slice = blockIdx.y;
     // The slice boundaries sit on even bodies so that j-pairs never straddle.
     const int64_t npairs = (n + 1) / 2;
@@ -84,7 +88,7 @@ __global__ void __launch_bounds__(kPPThreads)
     float4 pi[K];
 #pragma unroll
     for (int r = 0; r < K; ++r) {
-        const int64_t i = ib0 + tid + r * kPPThreads;
+        const int64_t i = ib0 + tid + r * T;
         pi[r] = i < n ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         nx[r] = f2(-pi[r].x, -pi[r].x);
         ny[r] = f2(-pi[r].y, -pi[r].y);
@@ -104,7 +108,6 @@ __global__ void __launch_bounds__(kPPThreads)
         const int stage = t % kPPStages;
         const int64_t jt = j0 + static_cast<int64_t>(t) * kPPTile;
         const int cnt = static_cast<int>((j1 - jt) < kPPTile ? (j1 - jt) : kPPTile);
-        if (cnt & 1) tile[stage][cnt] = make_float4(0.f, 0.f, 0.f, 0.f);  // pad the last pair: m = 0
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(&full[stage], static_cast<uint32_t>(cnt) * 16u);
         tma_bulk_g2s(&tile[stage][0], pos + jt, static_cast<uint32_t>(cnt) * 16u, &full[stage]);
@@ -119,19 +122,28 @@ __global__ void __launch_bounds__(kPPThreads)
         const int stage = t % kPPStages;
         const uint32_t parity = static_cast<uint32_t>(t / kPPStages) & 1u;
         const bool ok = mbar_wait_bounded(&full[stage], parity, status);
-        if (!__syncthreads_and(ok)) {
+        if (!__syncthreads_and(ok)) {  // also: every thread is done with `pairs`
             failed = true;
             break;
         }
         const int64_t jt = j0 + static_cast<int64_t>(t) * kPPTile;
         const int cnt = static_cast<int>((j1 - jt) < kPPTile ? (j1 - jt) : kPPTile);
-        const int cnt2 = (cnt + 1) & ~1;
-        const float4 *tl = tile[stage];
+        const int npr = (cnt + 1) >> 1;
+        // Re-lay the tile as j-pairs; an odd last body is paired with m = 0.
+        for (int q = tid; q < npr; q += T) {
+            const float4 a = tile[stage][2 * q];
+            const float4 b = (2 * q + 1 < cnt) ? tile[stage][2 * q + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+            pairs[2 * q] = make_float4(a.x, b.x, a.y, b.y);
+            pairs[2 * q + 1] = make_float4(a.z, b.z, a.w, b.w);
+        }
+        __syncthreads();  // pairs ready; tile[stage] is free again
+        if (tid == 0 && t + kPPStages < ntiles) issue(t + kPPStages);
+        const float4 *pr = pairs;
 #pragma unroll 2
-        for (int jj = 0; jj < cnt2; jj += 2) {
-            const float4 a = tl[jj];
-            const float4 b = tl[jj + 1];
-            const float2 xj = f2(a.x, b.x), yj = f2(a.y, b.y), zj = f2(a.z, b.z), mj = f2(a.w, b.w);
+        for (int q = 0; q < npr; ++q) {
+            const float4 u = pr[2 * q];
+            const float4 v = pr[2 * q + 1];
+            const float2 xj = f2(u.x, u.y), yj = f2(u.z, u.w), zj = f2(v.x, v.y), mj = f2(v.z, v.w);
 #pragma unroll
             for (int r = 0; r < K; ++r) {
                 const float2 dx = __fadd2_rn(xj, nx[r]);
@@ -152,8 +164,6 @@ __global__ void __launch_bounds__(kPPThreads)
                 az[r] = __ffma2_rn(dz, s, az[r]);
             }
         }
-        __syncthreads();  // every thread is done with this stage
-        if (tid == 0 && t + kPPStages < ntiles) issue(t + kPPStages);
     }
 
     if (failed) {
@@ -169,7 +179,7 @@ __global__ void __launch_bounds__(kPPThreads)
     if (nslices == 1) {
 #pragma unroll
         for (int r = 0; r < K; ++r) {
-            const int64_t i = ib0 + tid + r * kPPThreads;
+            const int64_t i = ib0 + tid + r * T;
             if (i >= n) continue;
             const float fx = ax[r].x + ax[r].y;
             const float fy = ay[r].x + ay[r].y;
@@ -185,7 +195,7 @@ __global__ void __launch_bounds__(kPPThreads)
     // result does not depend on which CTA ran when) and integrates.
 #pragma unroll
     for (int r = 0; r < K; ++r) {
-        const int64_t i = ib0 + tid + r * kPPThreads;
+        const int64_t i = ib0 + tid + r * T;
         if (i < n)
             partial[static_cast<int64_t>(slice) * n + i] =
                 make_float4(ax[r].x + ax[r].y, ay[r].x + ay[r].y, az[r].x + az[r].y, 0.f);
@@ -200,27 +210,29 @@ __global__ void __launch_bounds__(kPPThreads)
     __syncthreads();
     if (!last_cta) return;
     __threadfence();
-    float fx[K], fy[K], fz[K];
-#pragma unroll
-    for (int r = 0; r < K; ++r) fx[r] = fy[r] = fz[r] = 0.f;
-    for (int sl = 0; sl < nslices; ++sl) {
-#pragma unroll
-        for (int r = 0; r < K; ++r) {
-            const int64_t i = ib0 + tid + r * kPPThreads;
-            if (i < n) {
-                const float4 q = __ldcg(&partial[static_cast<int64_t>(sl) * n + i]);
-                fx[r] += q.x;
-                fy[r] += q.y;
-                fz[r] += q.z;
-            }
-        }
-    }
+    constexpr int kBatch = 8;  // partial loads in flight per body
 #pragma unroll
     for (int r = 0; r < K; ++r) {
-        const int64_t i = ib0 + tid + r * kPPThreads;
+        const int64_t i = ib0 + tid + r * T;
         if (i >= n) continue;
-        if (g.pos_out) integrate_body(i, pi[r], fx[r], fy[r], fz[r], g);
-        else if (g.force) g.force[i] = make_float4(fx[r], fy[r], fz[r], 0.f);
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        for (int sl0 = 0; sl0 < nslices; sl0 += kBatch) {
+            float4 q[kBatch];
+#pragma unroll
+            for (int b = 0; b < kBatch; ++b)
+                q[b] = (sl0 + b < nslices) ? __ldcg(&partial[static_cast<int64_t>(sl0 + b) * n + i])
+                                           : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int b = 0; b < kBatch; ++b) {
+                if (sl0 + b < nslices) {
+                    fx += q[b].x;
+                    fy += q[b].y;
+                    fz += q[b].z;
+                }
+            }
+        }
+        if (g.pos_out) integrate_body(i, pi[r], fx, fy, fz, g);
+        else if (g.force) g.force[i] = make_float4(fx, fy, fz, 0.f);
     }
 }
 
@@ -242,16 +254,16 @@ __global__ void unpack_kernel(const float4 *__restrict__ pos_mass, float4 *__res
 // ---------------------------------------------------------------- host side
 namespace {
 
-template <int K>
+template <int K, int T>
 int ctas_per_sm() {
     int c = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, pp_force_kernel<K, false>, kPPThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, pp_force_kernel<K, T, false>, T, 0);
     return c > 0 ? c : 1;
 }
 
 struct DeviceInfo {
     int sms = 0;
-    int cps[4] = {0, 0, 0, 0};  // CTAs per SM for K = 1, 2, 4, 8
+    int cps[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};  // CTAs per SM for T = 128, 256 and K = 1, 2, 4, 8
 };
 
 DeviceInfo device_info(int device) {
@@ -263,10 +275,14 @@ DeviceInfo device_info(int device) {
     if (!have[device]) {
         DeviceInfo d;
         cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, device);
-        d.cps[0] = ctas_per_sm<1>();
-        d.cps[1] = ctas_per_sm<2>();
-        d.cps[2] = ctas_per_sm<4>();
-        d.cps[3] = ctas_per_sm<8>();
+        d.cps[0][0] = ctas_per_sm<1, 128>();
+        d.cps[0][1] = ctas_per_sm<2, 128>();
+        d.cps[0][2] = ctas_per_sm<4, 128>();
+        d.cps[0][3] = ctas_per_sm<8, 128>();
+        d.cps[1][0] = ctas_per_sm<1, 256>();
+        d.cps[1][1] = ctas_per_sm<2, 256>();
+        d.cps[1][2] = ctas_per_sm<4, 256>();
+        d.cps[1][3] = ctas_per_sm<8, 256>();
         cache[device] = d;
         have[device] = true;
     }
@@ -280,18 +296,27 @@ int k_index(int k) { return k == 1 ? 0 : k == 2 ? 1 : k == 4 ? 2 : 3; }
 PPPlan pp_plan(int64_t n, int device) {
     PPPlan p;
     const DeviceInfo d = device_info(device);
-    int k = 4;
+    // Default shape from a sweep at N = 16,384 on GB300 (T x K in {128, 256} x
+    // {1, 2, 4, 8}): 256 threads with 2 i-bodies each was fastest.
+    int k = 2;
     if (const char *e = std::getenv("NBODY_PP_K")) {
         const int v = std::atoi(e);
         if (v == 1 || v == 2 || v == 4 || v == 8) k = v;
-    } else if (n <= 2 * kPPThreads) {
+    } else if (n <= 2 * kPPMinThreads) {
         k = 1;
     }
     p.k = k;
-    const int64_t per_block = static_cast<int64_t>(kPPThreads) * k;
+    int threads = n <= 2 * kPPMinThreads ? 128 : 256;
+    if (const char *e = std::getenv("NBODY_PP_THREADS")) {
+        const int v = std::atoi(e);
+        if (v == 128 || v == 256) threads = v;
+    }
+    p.threads = threads;
+    const int64_t per_block = static_cast<int64_t>(threads) * k;
     p.iblocks = static_cast<int>((n + per_block - 1) / per_block);
     const int64_t sms = d.sms > 0 ? d.sms : 1;
-    const int64_t cps = d.cps[k_index(k)] > 0 ? d.cps[k_index(k)] : 1;
+    const int ti = threads == 256 ? 1 : 0;
+    const int64_t cps = d.cps[ti][k_index(k)] > 0 ? d.cps[ti][k_index(k)] : 1;
     const int64_t npairs = (n + 1) / 2;
     // Slice count: each slice keeps at least one full tile of j-bodies. The
     // cost model charges every SM for the waves of CTAs it must run (a partial
@@ -324,17 +349,22 @@ PPPlan pp_plan(int64_t n, int device) {
     return p;
 }
 
+template <int K, int T>
+static cudaError_t launch_kt(const PPPlan &plan, const float4 *pos, int64_t n, float eps2, const Integrate &g,
+                             float4 *partial, unsigned *arrivals, cudaStream_t stream, int *status) {
+    const dim3 grid(plan.iblocks, plan.slices);
+    if (eps2 > 0.f)
+        pp_force_kernel<K, T, false><<<grid, T, 0, stream>>>(pos, n, eps2, plan.slices, partial, arrivals, g, status);
+    else
+        pp_force_kernel<K, T, true><<<grid, T, 0, stream>>>(pos, n, eps2, plan.slices, partial, arrivals, g, status);
+    return cudaGetLastError();
+}
+
 template <int K>
 static cudaError_t launch_k(const PPPlan &plan, const float4 *pos, int64_t n, float eps2, const Integrate &g,
                             float4 *partial, unsigned *arrivals, cudaStream_t stream, int *status) {
-    const dim3 grid(plan.iblocks, plan.slices);
-    if (eps2 > 0.f)
-        pp_force_kernel<K, false><<<grid, kPPThreads, 0, stream>>>(pos, n, eps2, plan.slices, partial, arrivals, g,
-                                                                    status);
-    else
-        pp_force_kernel<K, true><<<grid, kPPThreads, 0, stream>>>(pos, n, eps2, plan.slices, partial, arrivals, g,
-                                                                   status);
-    return cudaGetLastError();
+    if (plan.threads == 256) return launch_kt<K, 256>(plan, pos, n, eps2, g, partial, arrivals, stream, status);
+    return launch_kt<K, 128>(plan, pos, n, eps2, g, partial, arrivals, stream, status);
 }
 
 cudaError_t pp_launch(const PPPlan &plan, const float4 *pos, int64_t n, float eps2, const Integrate &g,

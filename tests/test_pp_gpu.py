@@ -119,11 +119,13 @@ def test_pp_slicing_does_not_change_forces(nb, cuda, monkeypatch):
     check_forces(out["32"], out["1"], rms_tol=1e-6, max_tol=1e-4)
 
 
+@pytest.mark.parametrize("threads", ["128", "256"])
 @pytest.mark.parametrize("k", ["1", "2", "4", "8"])
-def test_pp_bodies_per_thread_variants(nb, cuda, oracle, monkeypatch, k):
+def test_pp_bodies_per_thread_variants(nb, cuda, oracle, monkeypatch, k, threads):
     from nbody_gb300 import initializers as I
 
     monkeypatch.setenv("NBODY_PP_K", k)
+    monkeypatch.setenv("NBODY_PP_THREADS", threads)
     n = 3000
     pos, vel, mass = I.uniform_ball(n, seed=4)
     solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp")
