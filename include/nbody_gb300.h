@@ -116,6 +116,31 @@ int nbody_profile_read(nbody_ctx *ctx, double *ms, int *launches, int nstages);
 const char *nbody_stage_name(int stage);
 int nbody_stage_count(void);
 
+/* Direct-sum accelerations without any allocation by this library. It has
+ * no counterpart in the reference. It is for callers that cannot let a library
+ * call cudaMalloc: a frame or control loop that must not stall on an
+ * allocation (cudaMalloc / cudaFree can synchronise the device), or a host
+ * application that owns all device memory through its own pool. Same result
+ * as nbody_pp_forces_device (library layout, G = 1, squared softening eps2),
+ * enqueued on `stream` (a cudaStream_t; NULL = the legacy default stream) of
+ * the current device.
+ *
+ * Scratch: a fixed 8 MiB array in device memory inside this library, held on
+ * every GPU that loads it until the process exits; nothing else is
+ * allocated, by the library or on its behalf. n > NBODY_NOALLOC_MAX_BODIES
+ * returns NBODY_ERR_CAPACITY; for large n fewer j-slices are used so that
+ * the partial sums fit. The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture. Every call shares the one array: calls whose work overlaps on the
+ * GPU (several streams or host threads) race and must be serialised by the
+ * caller.
+ *
+ * kernel_status may be NULL; if given, the call waits for `stream` and
+ * stores the kernel's status there (NBODY_OK, or NBODY_ERR_TIMEOUT). */
+#define NBODY_NOALLOC_MAX_BODIES 4194304
+int nbody_pp_forces_noalloc(const void *pos_mass4, void *force4, int64_t n, float eps2, void *stream,
+                            int *kernel_status);
+
 #ifdef __cplusplus
 }
 #endif

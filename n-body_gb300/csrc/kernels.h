@@ -38,6 +38,10 @@ struct PPPlan {
 
 PPPlan pp_plan(int64_t n, int device);
 
+// pp_plan with the slice count lowered until the scratch it needs fits in
+// `scratch_bytes` (one slice needs none).
+PPPlan pp_plan_within(int64_t n, int device, size_t scratch_bytes);
+
 // Direct-sum forces at `pos` (float4 x,y,z,m) followed by the integrator
 // (or a plain force write when g.pos_out is null). When plan.slices > 1,
 // `scratch` must hold plan.partial_bytes and its first plan.arrivals_bytes

@@ -349,6 +349,19 @@ PPPlan pp_plan(int64_t n, int device) {
     return p;
 }
 
+PPPlan pp_plan_within(int64_t n, int device, size_t scratch_bytes) {
+    PPPlan p = pp_plan(n, device);
+    while (p.slices > 1 && p.partial_bytes > scratch_bytes) {
+        const int64_t fit = static_cast<int64_t>((scratch_bytes > p.arrivals_bytes ? scratch_bytes - p.arrivals_bytes : 0) /
+                                                 (static_cast<size_t>(n) * sizeof(float4)));
+        p.slices = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(fit, p.slices - 1)));
+        p.arrivals_bytes = p.slices > 1 ? p.arrivals_bytes : 0;
+        p.partial_bytes =
+            p.slices > 1 ? p.arrivals_bytes + static_cast<size_t>(p.slices) * static_cast<size_t>(n) * sizeof(float4) : 0;
+    }
+    return p;
+}
+
 template <int K, int T>
 static cudaError_t launch_kt(const PPPlan &plan, const float4 *pos, int64_t n, float eps2, const Integrate &g,
                              float4 *partial, unsigned *arrivals, cudaStream_t stream, int *status) {

@@ -57,6 +57,7 @@ SIGNATURES = {
     "nbody_profile_read": (_i, [_vp, ctypes.POINTER(ctypes.c_double), _ip, _i]),
     "nbody_stage_name": (ctypes.c_char_p, [_i]),
     "nbody_stage_count": (_i, []),
+    "nbody_pp_forces_noalloc": (_i, [_vp, _vp, _i64, _f, _vp, _ip]),
 }
 
 

@@ -1,0 +1,65 @@
+"""nbody_pp_forces_noalloc: the direct-sum entry point for callers that cannot
+let a library allocate device memory (a loop that must not stall on
+cudaMalloc/cudaFree, or an application whose own pool owns all device memory).
+Its scratch is a fixed array inside the library; the caller passes only input
+and output buffers.
+
+It is called through the C ABI twice in a row and compared with the
+allocating entry point (nbody_pp_forces_device) within the direct-sum force
+tolerance used by the other GPU tests: per-body relative error RMS <= 1e-5,
+max <= 1e-3. This file is collected last on purpose.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import rel_err_stats
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(got, ref):
+    rms, mx = rel_err_stats(got, ref)
+    assert rms <= 1e-5 and mx <= 1e-3, (rms, mx)
+
+
+@pytest.mark.parametrize("n", [16384, 5000])
+def test_noalloc_matches_allocating_entry_point_twice(nb, cuda, n):
+    torch = cuda
+    from nbody_gb300 import initializers as I
+
+    pos, vel, mass = I.uniform_ball(n, seed=77 + n)
+    pm = torch.from_numpy(I.pos_mass(pos, mass)).cuda()
+    stream = torch.cuda.Stream()
+    ref = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp")
+    solver.set_stream(stream.cuda_stream)
+    solver.pp_forces_device(pm, ref)
+    stream.synchronize()
+    ref_h = ref.cpu().numpy()
+    solver.close()
+
+    L = nb.lib()
+    outs = []
+    for _ in range(2):
+        out = torch.full((n, 4), float("nan"), dtype=torch.float32, device="cuda")
+        status = ctypes.c_int(-1)
+        rc = L.nbody_pp_forces_noalloc(pm.data_ptr(), out.data_ptr(), n, 40.0, stream.cuda_stream,
+                                       ctypes.byref(status))
+        assert rc == nb.OK, nb.status_string(rc)
+        assert status.value == nb.OK
+        got = out.cpu().numpy()
+        _check(got, ref_h)
+        assert np.all(got[:, 3] == 0)
+        outs.append(got)
+    # the shared scratch is cleared on every call: the second call repeats the first
+    np.testing.assert_array_equal(outs[0], outs[1])
+
+
+def test_noalloc_rejects_too_many_bodies(nb, cuda):
+    L = nb.lib()
+    n = 4194304 + 1
+    rc = L.nbody_pp_forces_noalloc(16, 16, n, 40.0, None, None)  # rejected before any device work
+    assert rc == nb.ERR_CAPACITY
+    assert L.nbody_pp_forces_noalloc(None, None, 10, 40.0, None, None) == nb.ERR_ARG
