@@ -87,8 +87,12 @@ int nbody_download(nbody_ctx *ctx, float *positions4, float *velocities4, float 
  * (NBODY_OK, or NBODY_ERR_TIMEOUT / NBODY_ERR_CAPACITY raised by a kernel). */
 int nbody_sync(nbody_ctx *ctx);
 
-/* Device pointers of the resident state (library layout, see above). */
+/* Device pointers of the resident state (library layout, see above). A
+ * Barnes-Hut context keeps its state in the order of its last Morton sort;
+ * nbody_device_order then gives the int array mapping each entry to the
+ * caller's body index (NULL while the state is still in the caller's order). */
 int nbody_device_state(nbody_ctx *ctx, void **pos_mass4, void **vel4, void **acc4);
+int nbody_device_order(nbody_ctx *ctx, void **ids);
 
 /* Direct-sum accelerations for n bodies on device buffers (library layout):
  * force4[i] = sum_j m_j (x_j - x_i) / (|x_j - x_i|^2 + eps2)^1.5, the -v 2
@@ -105,6 +109,32 @@ int nbody_pp_step_device(nbody_ctx *ctx, const void *pos_in, void *pos_out, void
 /* Launch shape the direct-sum kernel picked for n bodies: i-bodies per
  * thread, j-slices and CTAs. For tests and tuning reports. */
 int nbody_pp_config(nbody_ctx *ctx, int64_t n, int *bodies_per_thread, int *slices, int *ctas);
+
+/* Barnes-Hut pieces on device buffers (context's stream and workspace).
+ *
+ * nbody_bh_keys_device: the root box of n bodies (min xyz, max xyz; the
+ * reference's seeds, src/Octree/ParallelOctreeCPU.cpp:76-118) into box_out
+ * (6 floats, device) and their 63-bit Morton keys into keys_out (uint64,
+ * device): 21 bits per axis, x highest in each triple, quantised as
+ * src/shaders/ComputeShaders/morton.glsl:49-75 does with 2^21 cells per axis.
+ *
+ * nbody_sort_pairs_device: sorts (uint64 key, uint32 value) pairs by key in
+ * place, stably -- replaces src/shaders/ComputeShaders/bitonicSort.glsl:23-50.
+ *
+ * nbody_bh_forces_device: Barnes-Hut accelerations of n bodies (library
+ * layout, caller's order) with the context's eps2 and theta2: the
+ * acceleration -v 6 computes (ParticleSolverBHutCPUParallel.cpp:18-46 with
+ * Octree::computeGravityForce, src/Octree/Octree.cpp:303-338).
+ *
+ * nbody_bh_tree_export: the tree of the last Barnes-Hut build, in pre-order:
+ * *count records, of which the first min(cap, count) are copied to host as 8
+ * floats each (centre of mass x, y, z, mass, then as int32 bit patterns:
+ * side^2 (float, -1 for leaves), next record, first body, body count of a
+ * leaf); box_host (may be NULL) receives the root box. */
+int nbody_bh_keys_device(nbody_ctx *ctx, const void *pos_mass4, int64_t n, void *keys_out, void *box_out);
+int nbody_sort_pairs_device(nbody_ctx *ctx, void *keys, void *vals, int64_t n);
+int nbody_bh_forces_device(nbody_ctx *ctx, const void *pos_mass4, void *force4, int64_t n);
+int nbody_bh_tree_export(nbody_ctx *ctx, float *records_host, int64_t cap, int64_t *count, float *box_host);
 
 /* Per-stage timing. While enabled, every kernel stage launched by this
  * context is bracketed by a CUDA event pair on its launch stream.

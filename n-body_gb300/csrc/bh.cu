@@ -1,0 +1,661 @@
+// Barnes-Hut gravity for sm_103a: per-step bounding box, 63-bit Morton keys,
+// stable radix sort, state gather, octree from sorted keys, bottom-up mass /
+// centre of mass, and a warp-cooperative stackless traversal with the
+// reference's opening criterion and integrator fused in.
+//
+// Replaces the reference's -v 6 CPU path (ParticleSolverBHutCPUParallel,
+// src/ParticleSolver/ParticleSolverBHutCPUParallel/ParticleSolverBHutCPUParallel.cpp:18-41
+// over ParallelOctreeCPU, src/Octree/ParallelOctreeCPU.cpp) and the -v 7 GLSL
+// path (ParallelOctreeGPU + shaders #18-32).
+//
+// Tree. The reference inserts bodies one by one into an octree over the
+// per-step box, subdividing a leaf until its two bodies separate, then prunes
+// empty children (Octree.cpp:81-294). The cells it ends up with are the
+// dyadic cells of the box that hold >= 2 bodies (plus chains of cells with a
+// single occupied child, which a traversal treats exactly like their only
+// child) and single-body leaves. With the bodies sorted by 63-bit Morton key,
+// those cells are the octree levels L = floor(delta / 3) of a binary radix
+// tree over the keys (delta = common prefix length in bits; Karras 2012): a
+// radix-tree node is a cell top when its level exceeds its parent's. Cells
+// are laid out in depth-first pre-order, so a cell's first child is the next
+// record and `next` (the escape link of Octree.cpp:303-338) is the first
+// record after its subtree. For a body b let mask[b] be the set of levels of
+// cells whose first body is b and cnt[b] = |mask[b]| + (b is a lone body);
+// with P the exclusive prefix sum of cnt, the cells starting at b occupy
+// records P[b] .. in order of level and b's own leaf comes last; a cell whose
+// bodies are [lo, hi] has next = P[hi + 1]. Bodies with identical 63-bit keys
+// share one leaf record (a "bucket") and interact one by one.
+//
+// Cell geometry follows the reference bit for bit: a cell's box is the root
+// box halved level by level in FP32 as Octree::subdivide does
+// (Octree.cpp:159-231: w = max - min; centre = min + w / 2), and the opening
+// test is s*s < theta2 * d2 with s the largest side, d2 = dx*dx + dy*dy + dz*dz
+// evaluated without FMA contraction (Octree.cpp:303-338).
+#include <cuda_runtime.h>
+
+#include <cfloat>
+
+#include "bh.h"
+#include "common.cuh"
+#include "sort.h"
+
+namespace nbody {
+
+namespace {
+
+constexpr int kMaxLevel = 21;
+
+__device__ __forceinline__ int level_of(int delta) {
+    const int l = delta / 3;
+    return l < kMaxLevel ? l : kMaxLevel;
+}
+
+// ------------------------------------------------------------- bounding box
+// Reference seeds: min = FLT_MAX, max = FLT_MIN (ParallelOctreeCPU.cpp:77-82),
+// strict comparisons. min/max are order-independent, so the result is exact.
+__global__ void bbox_kernel(const float4 *__restrict__ pos, int64_t n, float *__restrict__ partial,
+                            unsigned *__restrict__ counter, float *__restrict__ box) {
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+    float mx[3] = {FLT_MIN, FLT_MIN, FLT_MIN};
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float4 p = pos[i];
+        if (p.x < mn[0]) mn[0] = p.x;
+        if (p.y < mn[1]) mn[1] = p.y;
+        if (p.z < mn[2]) mn[2] = p.z;
+        if (p.x > mx[0]) mx[0] = p.x;
+        if (p.y > mx[1]) mx[1] = p.y;
+        if (p.z > mx[2]) mx[2] = p.z;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float o1 = __shfl_down_sync(0xffffffffu, mn[a], off);
+            const float o2 = __shfl_down_sync(0xffffffffu, mx[a], off);
+            if (o1 < mn[a]) mn[a] = o1;
+            if (o2 > mx[a]) mx[a] = o2;
+        }
+    }
+    __shared__ float wm[32][6];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) {
+        for (int a = 0; a < 3; ++a) {
+            wm[warp][a] = mn[a];
+            wm[warp][3 + a] = mx[a];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < nw; ++w)
+            for (int a = 0; a < 3; ++a) {
+                if (wm[w][a] < wm[0][a]) wm[0][a] = wm[w][a];
+                if (wm[w][3 + a] > wm[0][3 + a]) wm[0][3 + a] = wm[w][3 + a];
+            }
+        for (int a = 0; a < 6; ++a) partial[blockIdx.x * 6 + a] = wm[0][a];
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        float r[6] = {FLT_MAX, FLT_MAX, FLT_MAX, FLT_MIN, FLT_MIN, FLT_MIN};
+        for (unsigned b = 0; b < gridDim.x; ++b)
+            for (int a = 0; a < 3; ++a) {
+                const float lo = __ldcg(&partial[b * 6 + a]);
+                const float hi = __ldcg(&partial[b * 6 + 3 + a]);
+                if (lo < r[a]) r[a] = lo;
+                if (hi > r[3 + a]) r[3 + a] = hi;
+            }
+        for (int a = 0; a < 6; ++a) box[a] = r[a];
+        *counter = 0u;
+    }
+}
+
+// ------------------------------------------------------------- Morton keys
+__device__ __forceinline__ uint64_t expand21(uint64_t v) {
+    v &= 0x1FFFFFull;
+    v = (v | (v << 32)) & 0x001F00000000FFFFull;
+    v = (v | (v << 16)) & 0x001F0000FF0000FFull;
+    v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+    v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+// morton.glsl:49-51,68-75 with 2^21 cells per axis, each step one IEEE op.
+__device__ __forceinline__ uint32_t quantize21(float p, float lo, float hi) {
+    float ext = __fsub_rn(hi, lo);
+    if (!(ext > 1e-6f)) ext = 1e-6f;
+    float t = __fdiv_rn(__fsub_rn(p, lo), ext);
+    if (t < 0.f) t = 0.f;
+    if (t > 1.f) t = 1.f;
+    float g = __fmul_rn(t, 2097152.0f);
+    if (g > 2097151.0f) g = 2097151.0f;
+    return __float2uint_rz(g);
+}
+
+__global__ void morton_kernel(const float4 *__restrict__ pos, int64_t n, const float *__restrict__ box,
+                              uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos[i];
+    const uint64_t qx = quantize21(p.x, box[0], box[3]);
+    const uint64_t qy = quantize21(p.y, box[1], box[4]);
+    const uint64_t qz = quantize21(p.z, box[2], box[5]);
+    keys[i] = (expand21(qx) << 2) | (expand21(qy) << 1) | expand21(qz);
+    if (vals) vals[i] = static_cast<uint32_t>(i);
+}
+
+// ------------------------------------------------------------------ gather
+__global__ void gather_kernel(const uint32_t *__restrict__ perm, int64_t n, const float4 *__restrict__ pos_in,
+                              const float4 *__restrict__ vel_in, const float4 *__restrict__ acc_in,
+                              const int *__restrict__ id_in, float4 *__restrict__ pos_out,
+                              float4 *__restrict__ vel_out, float4 *__restrict__ acc_out,
+                              int *__restrict__ id_out, int *status) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t j = perm[i];
+    if (j >= static_cast<uint64_t>(n)) {  // not a permutation: report, read in bounds
+        record_error(status, NBODY_ERR_CAPACITY);
+        j = 0;
+    }
+    pos_out[i] = pos_in[j];
+    if (vel_out) vel_out[i] = vel_in[j];
+    if (acc_out) acc_out[i] = acc_in[j];
+    if (id_out) id_out[i] = id_in ? id_in[j] : static_cast<int>(j);
+}
+
+// ------------------------------------------------------ binary radix tree
+__device__ __forceinline__ int delta_at(const uint64_t *__restrict__ k, int64_t n, int64_t i, int64_t j) {
+    if (j < 0 || j >= n) return -1;
+    const uint64_t a = k[i], b = k[j];
+    if (a != b) return __clzll(static_cast<long long>(a ^ b)) - 1;  // bit 63 is always 0
+    return 63 + __clz(static_cast<int>(i ^ j));                         // equal keys: break ties by index
+}
+
+__global__ void radix_tree_kernel(const uint64_t *__restrict__ k, int64_t n, BinaryTree t) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int dl = delta_at(k, n, i, i - 1), dr = delta_at(k, n, i, i + 1);
+    const int d = dr > dl ? 1 : -1;
+    const int dmin = d > 0 ? dl : dr;
+    int64_t lmax = 2;
+    while (delta_at(k, n, i, i + lmax * d) > dmin) lmax *= 2;
+    int64_t l = 0;
+    for (int64_t s = lmax / 2; s >= 1; s /= 2)
+        if (delta_at(k, n, i, i + (l + s) * d) > dmin) l += s;
+    const int64_t j = i + l * d;
+    const int dnode = delta_at(k, n, i, j);
+    int64_t s = 0;
+    int64_t step = l;
+    do {
+        step = (step + 1) >> 1;
+        if (delta_at(k, n, i, i + (s + step) * d) > dnode) s += step;
+    } while (step > 1);
+    const int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
+    const int64_t lo = i < j ? i : j, hi = i < j ? j : i;
+    const int left = (lo == gamma) ? ~static_cast<int>(gamma) : static_cast<int>(gamma);
+    const int right = (hi == gamma + 1) ? ~static_cast<int>(gamma + 1) : static_cast<int>(gamma + 1);
+    t.lo[i] = static_cast<int>(lo);
+    t.hi[i] = static_cast<int>(hi);
+    t.left[i] = left;
+    t.right[i] = right;
+    t.delta[i] = dnode;
+    if (left < 0) t.lparent[~left] = static_cast<int>(i); else t.iparent[left] = static_cast<int>(i);
+    if (right < 0) t.lparent[~right] = static_cast<int>(i); else t.iparent[right] = static_cast<int>(i);
+    if (i == 0) t.iparent[0] = -1;
+}
+
+// Cell tops: radix-tree nodes whose octree level exceeds their parent's.
+__global__ void mark_cells_kernel(int64_t n, BinaryTree t, uint32_t *__restrict__ mask) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int L = level_of(t.delta[i]);
+    const int Lp = i == 0 ? -1 : level_of(t.delta[t.iparent[i]]);
+    const bool top = L > Lp;
+    t.top[i] = top ? 1 : 0;
+    if (top) atomicOr(&mask[t.lo[i]], 1u << L);
+}
+
+__global__ void count_nodes_kernel(const uint64_t *__restrict__ k, int64_t n, const uint32_t *__restrict__ mask,
+                                   uint32_t *__restrict__ cnt) {
+    const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    const bool lone = !((b > 0 && k[b] == k[b - 1]) || (b + 1 < n && k[b] == k[b + 1]));
+    cnt[b] = __popc(mask[b]) + (lone ? 1u : 0u);
+}
+
+// Side^2 of the level-L cell holding `key`: the root box halved L times in
+// FP32 exactly as Octree::subdivide computes child boxes.
+__device__ __forceinline__ float cell_side2(uint64_t key, int L, const float *__restrict__ box) {
+    float mn[3] = {box[0], box[1], box[2]};
+    float mx[3] = {box[3], box[4], box[5]};
+    for (int l = 1; l <= L; ++l) {
+        const uint32_t dgt = static_cast<uint32_t>(key >> (63 - 3 * l)) & 7u;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float w = __fsub_rn(mx[a], mn[a]);
+            const float c = __fadd_rn(mn[a], __fmul_rn(w, 0.5f));
+            // key bit 1 = upper half [min + w/2, max]; 0 = lower half [min, min + w/2]
+            if ((dgt >> (2 - a)) & 1u) mn[a] = c; else mx[a] = c;
+        }
+    }
+    const float sx = __fsub_rn(mx[0], mn[0]), sy = __fsub_rn(mx[1], mn[1]), sz = __fsub_rn(mx[2], mn[2]);
+    const float sxy = sx < sy ? sy : sx;
+    const float s = sxy < sz ? sz : sxy;
+    return __fmul_rn(s, s);
+}
+
+__global__ void emit_cells_kernel(const uint64_t *__restrict__ k, int64_t n, BinaryTree t,
+                                  const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
+                                  const float *__restrict__ box, BHNode *__restrict__ nodes) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    if (!t.top[i]) {
+        t.top_index[i] = -1;
+        return;
+    }
+    const int L = level_of(t.delta[i]);
+    const int lo = t.lo[i], hi = t.hi[i];
+    const uint32_t idx = P[lo] + __popc(mask[lo] & ((1u << L) - 1u));
+    t.top_index[i] = static_cast<int>(idx);
+    int4 meta;
+    if (L < kMaxLevel) {
+        meta = make_int4(__float_as_int(cell_side2(k[lo], L, box)), static_cast<int>(P[hi + 1]), lo, 0);
+    } else {  // bucket of bodies with identical keys
+        meta = make_int4(__float_as_int(-1.f), static_cast<int>(P[hi + 1]), lo, hi - lo + 1);
+    }
+    nodes[idx].meta = meta;
+}
+
+__global__ void emit_leaves_kernel(const uint64_t *__restrict__ k, int64_t n, const float4 *__restrict__ pos,
+                                   const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
+                                   BHNode *__restrict__ nodes) {
+    const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    const bool lone = !((b > 0 && k[b] == k[b - 1]) || (b + 1 < n && k[b] == k[b + 1]));
+    if (!lone) return;
+    const uint32_t idx = P[b] + __popc(mask[b]);
+    nodes[idx].cm = pos[b];
+    nodes[idx].meta = make_int4(__float_as_int(-1.f), static_cast<int>(P[b + 1]), static_cast<int>(b), 1);
+}
+
+// Bottom-up mass and mass-weighted position sums over the radix tree; the
+// second child to arrive at a node combines both (left + right, fixed order).
+// Prefix lengths strictly grow from parent to child (at most 63 key bits plus
+// 32 tie-break bits), so no body climbs more than 96 nodes.
+constexpr int kMaxRadixDepth = 128;
+
+__global__ void upsweep_kernel(int64_t n, const float4 *__restrict__ pos, BinaryTree t,
+                               unsigned *__restrict__ arrivals, float4 *__restrict__ msum,
+                               BHNode *__restrict__ nodes, int *status) {
+    const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (b >= n || n < 2) return;
+    int p = t.lparent[b];
+    for (int depth = 0; p >= 0; ++depth) {
+        if (depth >= kMaxRadixDepth) {
+            record_error(status, NBODY_ERR_CAPACITY);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&arrivals[p], 1u) == 0u) return;
+        __threadfence();
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        const int ch[2] = {t.left[p], t.right[p]};
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            float4 v;
+            if (ch[c] < 0) {
+                const float4 q = pos[~ch[c]];
+                v = make_float4(q.x * q.w, q.y * q.w, q.z * q.w, q.w);
+            } else {
+                v = __ldcg(&msum[ch[c]]);
+            }
+            acc.x += v.x;
+            acc.y += v.y;
+            acc.z += v.z;
+            acc.w += v.w;
+        }
+        msum[p] = acc;
+        const int idx = t.top_index[p];
+        if (idx >= 0) {
+            const float m = acc.w;
+            nodes[idx].cm = m > 0.f ? make_float4(acc.x / m, acc.y / m, acc.z / m, m) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        p = t.iparent[p];
+    }
+}
+
+// --------------------------------------------------------------- traversal
+// One warp walks the pre-order records of the tree for its 32 bodies. A lane
+// evaluates the reference criterion on each record it has not already
+// covered (skip <= i); an accepted record adds its force and sets skip to
+// the record's `next`. The warp descends (i + 1) if any lane opened the
+// record, otherwise it jumps to the smallest `skip` of its lanes. Every lane
+// therefore sees exactly the records its own reference walk would accept.
+__global__ void __launch_bounds__(256) traverse_kernel(const BHNode *__restrict__ nodes,
+                                                       const uint32_t *__restrict__ node_total,
+                                                       const float4 *__restrict__ pos, int64_t n, float eps2,
+                                                       float theta2, float dt, float4 *__restrict__ pos_out,
+                                                       float4 *__restrict__ vel, float4 *__restrict__ acc,
+                                                       float4 *__restrict__ force_out, const int *__restrict__ ids) {
+    const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const bool valid = b < n;
+    const int m_nodes = static_cast<int>(*node_total);
+    const float4 me = valid ? pos[b] : make_float4(0.f, 0.f, 0.f, 0.f);
+    int skip = valid ? 0 : m_nodes;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    int i = 0;
+    while (i < m_nodes) {
+        const float4 cm = __ldg(&nodes[i].cm);
+        const int4 meta = __ldg(&nodes[i].meta);
+        bool open = false;
+        if (skip <= i) {
+            const float dx = __fsub_rn(cm.x, me.x), dy = __fsub_rn(cm.y, me.y), dz = __fsub_rn(cm.z, me.z);
+            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            const float s2 = __int_as_float(meta.x);
+            if (s2 < 0.f || s2 < __fmul_rn(theta2, d2)) {
+                if (meta.w >= 2) {
+                    const int q1 = meta.z + meta.w < n ? meta.z + meta.w : static_cast<int>(n);
+                    for (int q = meta.z < 0 ? 0 : meta.z; q < q1; ++q) {
+                        const float4 o = pos[q];
+                        const float ex = o.x - me.x, ey = o.y - me.y, ez = o.z - me.z;
+                        const float e2 = __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
+                        if (o.w > 0.f && e2 > 0.f) {
+                            const float inv = rsqrt_ftz(e2 + eps2);
+                            const float w = o.w * inv * inv * inv;
+                            fx = fmaf(ex, w, fx);
+                            fy = fmaf(ey, w, fy);
+                            fz = fmaf(ez, w, fz);
+                        }
+                    }
+                } else if (cm.w > 0.f && d2 > 0.f) {
+                    const float inv = rsqrt_ftz(d2 + eps2);
+                    const float w = cm.w * inv * inv * inv;
+                    fx = fmaf(dx, w, fx);
+                    fy = fmaf(dy, w, fy);
+                    fz = fmaf(dz, w, fz);
+                }
+                skip = meta.y;
+            } else {
+                open = true;
+            }
+        }
+        if (__any_sync(0xffffffffu, open)) {
+            ++i;
+        } else {
+            // Every `next` lies beyond its record; max() keeps the walk finite
+            // (at most m_nodes iterations) whatever the records hold.
+            const int nx = static_cast<int>(__reduce_min_sync(0xffffffffu, static_cast<unsigned>(skip)));
+            i = nx > i ? nx : i + 1;
+        }
+    }
+    if (!valid) return;
+    const float4 anew = make_float4(fx, fy, fz, 0.f);
+    if (pos_out) {
+        // Reference integrator (include/ParticleSystem.h:52-69), no contraction.
+        const float h = __fmul_rn(dt, 0.5f);
+        float4 v = vel[b];
+        const float4 a = acc[b];
+        float4 p = me;
+        v.x = __fadd_rn(v.x, __fmul_rn(a.x, h));
+        v.y = __fadd_rn(v.y, __fmul_rn(a.y, h));
+        v.z = __fadd_rn(v.z, __fmul_rn(a.z, h));
+        p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
+        p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+        p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
+        v.x = __fadd_rn(v.x, __fmul_rn(fx, h));
+        v.y = __fadd_rn(v.y, __fmul_rn(fy, h));
+        v.z = __fadd_rn(v.z, __fmul_rn(fz, h));
+        pos_out[b] = p;
+        vel[b] = v;
+        acc[b] = anew;
+    }
+    if (force_out) {
+        const int d = ids ? ids[b] : static_cast<int>(b);
+        if (d >= 0 && d < n) force_out[d] = anew;
+    }
+}
+
+// out[ids[i]] = in[i] (back to the caller's body order), positions with w = 0.
+__global__ void unpermute_kernel(const int *__restrict__ ids, int64_t n, const float4 *__restrict__ in,
+                                 float4 *__restrict__ out, int zero_w, int *status) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 v = in[i];
+    if (zero_w) v.w = 0.f;
+    const int d = ids[i];
+    if (d < 0 || d >= n) {
+        record_error(status, NBODY_ERR_CAPACITY);
+        return;
+    }
+    out[d] = v;
+}
+
+// exclusive scan of cnt[0..n) into P[0..n], P[n] = total (three phases).
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(const uint32_t *__restrict__ in, int64_t n,
+                                                                  uint32_t *__restrict__ out,
+                                                                  uint32_t *__restrict__ tile_sums) {
+    __shared__ uint32_t warp_sums[32];
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t run = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+        v[j] = base + j < n ? in[base + j] : 0u;
+        const uint32_t t2 = v[j];
+        v[j] = run;
+        run += t2;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = run;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sums[lane];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += y;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t offset = (x - run) + (warp > 0 ? warp_sums[warp - 1] : 0u);
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j)
+        if (base + j < n) out[base + j] = v[j] + offset;
+    if (threadIdx.x == kScanThreads - 1) tile_sums[blockIdx.x] = offset + run;
+}
+
+__global__ void __launch_bounds__(1024) scan_sums_kernel(uint32_t *__restrict__ tile_sums, int tiles,
+                                                         uint32_t *__restrict__ total_out) {
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < tiles; base += 1024) {
+        const int i = base + threadIdx.x;
+        const uint32_t v = i < tiles ? tile_sums[i] : 0u;
+        uint32_t x = v;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += y;
+        }
+        __shared__ uint32_t ws[32];
+        if (lane == 31) ws[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = ws[lane];
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+                if (lane >= off) w += y;
+            }
+            ws[lane] = w;
+        }
+        __syncthreads();
+        const uint32_t incl = x + (warp > 0 ? ws[warp - 1] : 0u);
+        if (i < tiles) tile_sums[i] = carry + incl - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total_out = carry;
+}
+
+__global__ void scan_add_kernel(uint32_t *__restrict__ out, int64_t n, const uint32_t *__restrict__ tile_sums) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] += tile_sums[i / kScanTile];
+}
+
+unsigned grid_for(int64_t n, int threads) { return static_cast<unsigned>((n + threads - 1) / threads); }
+
+}  // namespace
+
+// ------------------------------------------------------------------- host
+size_t bh_workspace_bytes(int64_t n) {
+    BHWorkspace w;
+    return bh_workspace_layout(n, nullptr, &w);
+}
+
+size_t bh_workspace_layout(int64_t n, void *base, BHWorkspace *w) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> void * {
+        off = (off + 255) & ~static_cast<size_t>(255);
+        void *p = base ? static_cast<char *>(base) + off : nullptr;
+        off += bytes;
+        return p;
+    };
+    const size_t nn = static_cast<size_t>(n > 1 ? n : 2);
+    const int64_t tiles = (n + kScanTile - 1) / kScanTile;
+    w->n = n;
+    w->keys[0] = static_cast<uint64_t *>(take(sizeof(uint64_t) * nn));
+    w->keys[1] = static_cast<uint64_t *>(take(sizeof(uint64_t) * nn));
+    w->vals[0] = static_cast<uint32_t *>(take(sizeof(uint32_t) * nn));
+    w->vals[1] = static_cast<uint32_t *>(take(sizeof(uint32_t) * nn));
+    w->sort_scratch = take(sort_scratch_bytes(n));
+    w->box = static_cast<float *>(take(sizeof(float) * 8));
+    w->bbox_partial = static_cast<float *>(take(sizeof(float) * 6 * kBBoxBlocks));
+    w->bbox_counter = static_cast<unsigned *>(take(sizeof(unsigned) * 4));
+    w->tree.lo = static_cast<int *>(take(sizeof(int) * nn));
+    w->tree.hi = static_cast<int *>(take(sizeof(int) * nn));
+    w->tree.left = static_cast<int *>(take(sizeof(int) * nn));
+    w->tree.right = static_cast<int *>(take(sizeof(int) * nn));
+    w->tree.delta = static_cast<int *>(take(sizeof(int) * nn));
+    w->tree.iparent = static_cast<int *>(take(sizeof(int) * nn));
+    w->tree.lparent = static_cast<int *>(take(sizeof(int) * nn));
+    w->tree.top = static_cast<int *>(take(sizeof(int) * nn));
+    w->tree.top_index = static_cast<int *>(take(sizeof(int) * nn));
+    w->arrivals = static_cast<unsigned *>(take(sizeof(unsigned) * nn));
+    w->msum = static_cast<float4 *>(take(sizeof(float4) * nn));
+    w->mask = static_cast<uint32_t *>(take(sizeof(uint32_t) * nn));
+    w->cnt = static_cast<uint32_t *>(take(sizeof(uint32_t) * nn));
+    w->P = static_cast<uint32_t *>(take(sizeof(uint32_t) * (nn + 1)));
+    w->scan_sums = static_cast<uint32_t *>(take(sizeof(uint32_t) * static_cast<size_t>(tiles + 1)));
+    w->nodes = static_cast<BHNode *>(take(sizeof(BHNode) * 2 * nn));
+    w->node_count_host = 0;
+    return (off + 255) & ~static_cast<size_t>(255);
+}
+
+cudaError_t bh_bbox(const float4 *pos, int64_t n, BHWorkspace &w, cudaStream_t st, StageTimer *timer) {
+    if (timer) timer->begin(kStageBBox, st);
+    int blocks = static_cast<int>((n + 255) / 256);
+    if (blocks > kBBoxBlocks) blocks = kBBoxBlocks;
+    if (blocks < 1) blocks = 1;
+    bbox_kernel<<<blocks, 256, 0, st>>>(pos, n, w.bbox_partial, w.bbox_counter, w.box);
+    if (timer) timer->end(kStageBBox, st);
+    return cudaGetLastError();
+}
+
+cudaError_t bh_keys(const float4 *pos, int64_t n, BHWorkspace &w, cudaStream_t st, StageTimer *timer) {
+    if (timer) timer->begin(kStageMorton, st);
+    morton_kernel<<<grid_for(n, 256), 256, 0, st>>>(pos, n, w.box, w.keys[0], w.vals[0]);
+    if (timer) timer->end(kStageMorton, st);
+    return cudaGetLastError();
+}
+
+cudaError_t bh_sort(int64_t n, BHWorkspace &w, cudaStream_t st, int *status, StageTimer *timer) {
+    if (timer) timer->begin(kStageSort, st);
+    int alt = 0;
+    cudaError_t e = sort_pairs(w.keys[0], w.vals[0], w.keys[1], w.vals[1], n, w.sort_scratch, st, status, &alt);
+    if (timer) timer->end(kStageSort, st);
+    if (e != cudaSuccess) return e;
+    if (alt) {  // keep the sorted pairs in slot 0
+        uint64_t *tk = w.keys[0]; w.keys[0] = w.keys[1]; w.keys[1] = tk;
+        uint32_t *tv = w.vals[0]; w.vals[0] = w.vals[1]; w.vals[1] = tv;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t bh_gather(int64_t n, const BHWorkspace &w, const float4 *pos_in, const float4 *vel_in,
+                      const float4 *acc_in, const int *id_in, float4 *pos_out, float4 *vel_out, float4 *acc_out,
+                      int *id_out, cudaStream_t st, int *status, StageTimer *timer) {
+    if (timer) timer->begin(kStageGather, st);
+    gather_kernel<<<grid_for(n, 256), 256, 0, st>>>(w.vals[0], n, pos_in, vel_in, acc_in, id_in, pos_out, vel_out,
+                                                    acc_out, id_out, status);
+    if (timer) timer->end(kStageGather, st);
+    return cudaGetLastError();
+}
+
+cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaStream_t st, int *status,
+                     StageTimer *timer) {
+    if (timer) timer->begin(kStageBuild, st);
+    const uint64_t *k = w.keys[0];
+    cudaError_t e = cudaMemsetAsync(w.mask, 0, sizeof(uint32_t) * static_cast<size_t>(n), st);
+    if (e != cudaSuccess) return e;
+    if (n >= 2) {
+        radix_tree_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(k, n, w.tree);
+        mark_cells_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(n, w.tree, w.mask);
+    }
+    count_nodes_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, w.mask, w.cnt);
+    const int tiles = static_cast<int>((n + kScanTile - 1) / kScanTile);
+    scan_tiles_kernel<<<tiles, kScanThreads, 0, st>>>(w.cnt, n, w.P, w.scan_sums);
+    scan_sums_kernel<<<1, 1024, 0, st>>>(w.scan_sums, tiles, w.P + n);
+    scan_add_kernel<<<grid_for(n, 256), 256, 0, st>>>(w.P, n, w.scan_sums);
+    if (n >= 2)
+        emit_cells_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(k, n, w.tree, w.mask, w.P, w.box, w.nodes);
+    emit_leaves_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.mask, w.P, w.nodes);
+    if (timer) timer->end(kStageBuild, st);
+    if (timer) timer->begin(kStageUpsweep, st);
+    if (n >= 2) {
+        e = cudaMemsetAsync(w.arrivals, 0, sizeof(unsigned) * static_cast<size_t>(n - 1), st);
+        if (e != cudaSuccess) return e;
+        upsweep_kernel<<<grid_for(n, 256), 256, 0, st>>>(n, pos_sorted, w.tree, w.arrivals, w.msum, w.nodes,
+                                                         status);
+    }
+    if (timer) timer->end(kStageUpsweep, st);
+    return cudaGetLastError();
+}
+
+cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,
+                        float dt, float4 *pos_out, float4 *vel, float4 *acc, float4 *force_out, const int *ids,
+                        cudaStream_t st, StageTimer *timer) {
+    if (timer) timer->begin(kStageTraverse, st);
+    // The record count P[n] stays on the device; the kernel reads it.
+    traverse_kernel<<<grid_for(n, 256), 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel,
+                                                      acc, force_out, ids);
+    if (timer) timer->end(kStageTraverse, st);
+    return cudaGetLastError();
+}
+
+cudaError_t bh_unpermute(const int *ids, int64_t n, const float4 *in, float4 *out, bool zero_w, cudaStream_t st,
+                         int *status) {
+    unpermute_kernel<<<grid_for(n, 256), 256, 0, st>>>(ids, n, in, out, zero_w ? 1 : 0, status);
+    return cudaGetLastError();
+}
+
+}  // namespace nbody

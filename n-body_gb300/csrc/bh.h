@@ -1,0 +1,71 @@
+// Barnes-Hut pipeline internals (bounding box, keys, sort, gather, tree,
+// upsweep, traversal); internal to the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.h"
+
+namespace nbody {
+
+constexpr int kBBoxBlocks = 1024;
+
+// One pre-order tree record (32 bytes). cm = centre of mass and mass (for a
+// lone-body leaf: its position and mass). meta.x = s^2 of the cell as float
+// bits (-1 for leaves), meta.y = next record after the subtree, meta.z =
+// first body (sorted order), meta.w = body count of a leaf (0 for cells).
+struct __align__(16) BHNode {
+    float4 cm;
+    int4 meta;
+};
+
+// Binary radix tree over sorted keys: internal node i covers bodies
+// [lo, hi]; a child < 0 is body ~child.
+struct BinaryTree {
+    int *lo, *hi, *left, *right, *delta, *iparent, *lparent, *top, *top_index;
+};
+
+struct BHWorkspace {
+    int64_t n = 0;
+    uint64_t *keys[2] = {nullptr, nullptr};
+    uint32_t *vals[2] = {nullptr, nullptr};
+    void *sort_scratch = nullptr;
+    float *box = nullptr;  // min xyz, max xyz
+    float *bbox_partial = nullptr;
+    unsigned *bbox_counter = nullptr;
+    BinaryTree tree{};
+    unsigned *arrivals = nullptr;
+    float4 *msum = nullptr;
+    uint32_t *mask = nullptr;
+    uint32_t *cnt = nullptr;
+    uint32_t *P = nullptr;  // n + 1 entries; P[n] = record count
+    uint32_t *scan_sums = nullptr;
+    BHNode *nodes = nullptr;  // up to 2n records
+    int64_t node_count_host = 0;
+};
+
+// Bytes of device memory for a workspace of n bodies, and its layout inside
+// `base` (base == nullptr only computes the size). The bbox counter must be
+// zero before first use.
+size_t bh_workspace_bytes(int64_t n);
+size_t bh_workspace_layout(int64_t n, void *base, BHWorkspace *w);
+
+cudaError_t bh_bbox(const float4 *pos, int64_t n, BHWorkspace &w, cudaStream_t st, StageTimer *timer);
+cudaError_t bh_keys(const float4 *pos, int64_t n, BHWorkspace &w, cudaStream_t st, StageTimer *timer);
+cudaError_t bh_sort(int64_t n, BHWorkspace &w, cudaStream_t st, int *status, StageTimer *timer);
+cudaError_t bh_gather(int64_t n, const BHWorkspace &w, const float4 *pos_in, const float4 *vel_in,
+                      const float4 *acc_in, const int *id_in, float4 *pos_out, float4 *vel_out, float4 *acc_out,
+                      int *id_out, cudaStream_t st, int *status, StageTimer *timer);
+cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaStream_t st, int *status,
+                     StageTimer *timer);
+// Forces for every sorted body; with pos_out set, also the reference
+// integrator (pos_out must not alias pos_sorted). force_out, if set, receives
+// the acceleration at index ids[b] (or b when ids is null).
+cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,
+                        float dt, float4 *pos_out, float4 *vel, float4 *acc, float4 *force_out, const int *ids,
+                        cudaStream_t st, StageTimer *timer);
+cudaError_t bh_unpermute(const int *ids, int64_t n, const float4 *in, float4 *out, bool zero_w, cudaStream_t st,
+                         int *status);
+
+}  // namespace nbody

@@ -14,8 +14,10 @@
 #include <string>
 #include <vector>
 
+#include "bh.h"
 #include "kernels.h"
 #include "nbody_gb300.h"
+#include "sort.h"
 
 namespace {
 
@@ -91,6 +93,22 @@ struct nbody_ctx {
     bool uploaded = false;
     EventTimer *timer = nullptr;  // non-null while profiling is enabled
     std::string last_error;
+
+    // Barnes-Hut resident state, kept in the order of the last sort: pos[bh_pos],
+    // vel2[bh_va] / acc2[bh_va] and ids[bh_va] (ids[k] = caller's body index).
+    float4 *vel2[2] = {nullptr, nullptr};
+    float4 *acc2[2] = {nullptr, nullptr};
+    int *ids[2] = {nullptr, nullptr};
+    int bh_pos = 0, bh_va = 0;
+    bool ids_valid = false;  // false until the first step after an upload
+    // Barnes-Hut workspace (keys, sort scratch, tree), grown on demand.
+    void *ws_mem = nullptr;
+    size_t ws_bytes = 0;
+    nbody::BHWorkspace ws;
+    // Buffers for the device-pointer Barnes-Hut entry point.
+    float4 *dev_pos = nullptr;
+    int *dev_ids = nullptr;
+    int64_t dev_cap = 0;
 };
 
 namespace {
@@ -165,6 +183,50 @@ int pp_steps(nbody_ctx *ctx, int steps) {
     return NBODY_OK;
 }
 
+int ensure_workspace(nbody_ctx *ctx, int64_t n) {
+    if (ctx->ws_mem && ctx->ws.n >= n) return NBODY_OK;
+    const size_t bytes = nbody::bh_workspace_bytes(n);
+    if (ctx->ws_mem) {
+        NB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->ws_mem);
+        ctx->ws_mem = nullptr;
+    }
+    NB_CK(ctx, cudaMalloc(&ctx->ws_mem, bytes));
+    NB_CK(ctx, cudaMemsetAsync(ctx->ws_mem, 0, bytes, ctx->stream));
+    ctx->ws_bytes = bytes;
+    nbody::bh_workspace_layout(n, ctx->ws_mem, &ctx->ws);
+    return NBODY_OK;
+}
+
+// One Barnes-Hut step on the resident state (see nbody_ctx for the layout).
+int bh_step(nbody_ctx *ctx) {
+    nbody::BHWorkspace &w = ctx->ws;
+    const int64_t n = ctx->n;
+    float4 *P = ctx->pos[ctx->bh_pos], *Po = ctx->pos[ctx->bh_pos ^ 1];
+    float4 *V = ctx->vel2[ctx->bh_va], *Vo = ctx->vel2[ctx->bh_va ^ 1];
+    float4 *A = ctx->acc2[ctx->bh_va], *Ao = ctx->acc2[ctx->bh_va ^ 1];
+    const int *I = ctx->ids_valid ? ctx->ids[ctx->bh_va] : nullptr;
+    int *Io = ctx->ids[ctx->bh_va ^ 1];
+    nbody::StageTimer *tm = ctx->timer;
+    NB_CK(ctx, nbody::bh_bbox(P, n, w, ctx->stream, tm));
+    NB_CK(ctx, nbody::bh_keys(P, n, w, ctx->stream, tm));
+    NB_CK(ctx, nbody::bh_sort(n, w, ctx->stream, ctx->status, tm));
+    NB_CK(ctx, nbody::bh_gather(n, w, P, V, A, I, Po, Vo, Ao, Io, ctx->stream, ctx->status, tm));
+    NB_CK(ctx, nbody::bh_build(Po, n, w, ctx->stream, ctx->status, tm));
+    // New positions go to the buffer the gather just read from.
+    NB_CK(ctx, nbody::bh_traverse(Po, n, w, ctx->eps2, ctx->theta2, ctx->dt, P, Vo, Ao, nullptr, nullptr,
+                                  ctx->stream, tm));
+    ctx->bh_va ^= 1;
+    ctx->ids_valid = true;
+    return NBODY_OK;
+}
+
+int bh_steps(nbody_ctx *ctx, int steps) {
+    int rc = ensure_workspace(ctx, ctx->n);
+    for (int s = 0; rc == NBODY_OK && s < steps; ++s) rc = bh_step(ctx);
+    return rc;
+}
+
 }  // namespace
 
 extern "C" {
@@ -212,11 +274,20 @@ int nbody_create(nbody_ctx **out, int device, int mode, int64_t n, float dt, flo
     alloc(reinterpret_cast<void **>(&ctx->acc), b4);
     alloc(reinterpret_cast<void **>(&ctx->stage), 2 * b4);
     alloc(reinterpret_cast<void **>(&ctx->status), sizeof(int));
+    if (mode == NBODY_MODE_BH) {
+        ctx->vel2[0] = ctx->vel;
+        ctx->acc2[0] = ctx->acc;
+        alloc(reinterpret_cast<void **>(&ctx->vel2[1]), b4);
+        alloc(reinterpret_cast<void **>(&ctx->acc2[1]), b4);
+        alloc(reinterpret_cast<void **>(&ctx->ids[0]), sizeof(int) * static_cast<size_t>(n));
+        alloc(reinterpret_cast<void **>(&ctx->ids[1]), sizeof(int) * static_cast<size_t>(n));
+    }
     if (rc == NBODY_OK) {
         cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) rc = fail(ctx, e);
         ctx->stream = ctx->own_stream;
     }
+    if (rc == NBODY_OK && mode == NBODY_MODE_BH) rc = ensure_workspace(ctx, n);
     if (rc == NBODY_OK) {
         cudaError_t e = cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -242,6 +313,13 @@ int nbody_destroy(nbody_ctx *ctx) {
         cudaFree(ctx->stage);
         cudaFree(ctx->status);
         cudaFree(ctx->scratch);
+        cudaFree(ctx->vel2[1]);
+        cudaFree(ctx->acc2[1]);
+        cudaFree(ctx->ids[0]);
+        cudaFree(ctx->ids[1]);
+        cudaFree(ctx->ws_mem);
+        cudaFree(ctx->dev_pos);
+        cudaFree(ctx->dev_ids);
         delete ctx->timer;
         if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     }
@@ -273,6 +351,9 @@ int nbody_upload(nbody_ctx *ctx, const float *positions4, const float *velocitie
     else
         NB_CK(ctx, cudaMemsetAsync(ctx->acc, 0, b4, ctx->stream));
     ctx->cur = 0;
+    ctx->bh_pos = 0;
+    ctx->bh_va = 0;
+    ctx->ids_valid = false;
     NB_CK(ctx, nbody::pack_state(ctx->stage, ctx->stage + ctx->n, ctx->pos[0], ctx->n, ctx->stream));
     ctx->uploaded = true;
     return NBODY_OK;
@@ -283,7 +364,7 @@ int nbody_step(nbody_ctx *ctx, int steps) {
     if (!ctx->uploaded) return NBODY_ERR_STATE;
     DeviceGuard dg(ctx->device);
     if (ctx->mode == NBODY_MODE_PP) return pp_steps(ctx, steps);
-    return NBODY_ERR_ARG;
+    return bh_steps(ctx, steps);
 }
 
 int nbody_download(nbody_ctx *ctx, float *positions4, float *velocities4, float *accelerations4, float *forces4) {
@@ -291,14 +372,36 @@ int nbody_download(nbody_ctx *ctx, float *positions4, float *velocities4, float 
     if (!ctx->uploaded) return NBODY_ERR_STATE;
     DeviceGuard dg(ctx->device);
     const size_t b4 = static_cast<size_t>(ctx->n) * sizeof(float4);
+    const int64_t n = ctx->n;
+    if (ctx->mode == NBODY_MODE_BH && ctx->ids_valid) {
+        // Resident state is in the last sort's order: scatter back by id.
+        const int *ids = ctx->ids[ctx->bh_va];
+        float4 *half[2] = {ctx->stage, ctx->stage + n};
+        int h = 0;
+        auto out = [&](const float4 *src, float *dst, bool zero_w) -> int {
+            if (!dst) return NBODY_OK;
+            NB_CK(ctx, nbody::bh_unpermute(ids, n, src, half[h], zero_w, ctx->stream, ctx->status));
+            NB_CK(ctx, cudaMemcpyAsync(dst, half[h], b4, cudaMemcpyDeviceToHost, ctx->stream));
+            h ^= 1;
+            return NBODY_OK;
+        };
+        int rc = out(ctx->pos[ctx->bh_pos], positions4, true);
+        if (rc == NBODY_OK) rc = out(ctx->vel2[ctx->bh_va], velocities4, false);
+        if (rc == NBODY_OK) rc = out(ctx->acc2[ctx->bh_va], accelerations4, false);
+        if (rc == NBODY_OK) rc = out(ctx->acc2[ctx->bh_va], forces4, false);
+        if (rc != NBODY_OK) return rc;
+        return read_status(ctx);
+    }
+    float4 *pos = ctx->mode == NBODY_MODE_BH ? ctx->pos[ctx->bh_pos] : ctx->pos[ctx->cur];
+    float4 *vel = ctx->mode == NBODY_MODE_BH ? ctx->vel2[ctx->bh_va] : ctx->vel;
+    float4 *acc = ctx->mode == NBODY_MODE_BH ? ctx->acc2[ctx->bh_va] : ctx->acc;
     if (positions4) {
-        NB_CK(ctx, nbody::unpack_positions(ctx->pos[ctx->cur], ctx->stage, ctx->n, ctx->stream));
+        NB_CK(ctx, nbody::unpack_positions(pos, ctx->stage, ctx->n, ctx->stream));
         NB_CK(ctx, cudaMemcpyAsync(positions4, ctx->stage, b4, cudaMemcpyDeviceToHost, ctx->stream));
     }
-    if (velocities4) NB_CK(ctx, cudaMemcpyAsync(velocities4, ctx->vel, b4, cudaMemcpyDeviceToHost, ctx->stream));
-    if (accelerations4)
-        NB_CK(ctx, cudaMemcpyAsync(accelerations4, ctx->acc, b4, cudaMemcpyDeviceToHost, ctx->stream));
-    if (forces4) NB_CK(ctx, cudaMemcpyAsync(forces4, ctx->acc, b4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (velocities4) NB_CK(ctx, cudaMemcpyAsync(velocities4, vel, b4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (accelerations4) NB_CK(ctx, cudaMemcpyAsync(accelerations4, acc, b4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (forces4) NB_CK(ctx, cudaMemcpyAsync(forces4, acc, b4, cudaMemcpyDeviceToHost, ctx->stream));
     return read_status(ctx);
 }
 
@@ -319,9 +422,101 @@ int nbody_update_host(nbody_ctx *ctx, float *positions4, float *velocities4, flo
 
 int nbody_device_state(nbody_ctx *ctx, void **pos_mass4, void **vel4, void **acc4) {
     if (!ctx) return NBODY_ERR_ARG;
-    if (pos_mass4) *pos_mass4 = ctx->pos[ctx->cur];
-    if (vel4) *vel4 = ctx->vel;
-    if (acc4) *acc4 = ctx->acc;
+    const bool bh = ctx->mode == NBODY_MODE_BH;
+    if (pos_mass4) *pos_mass4 = bh ? ctx->pos[ctx->bh_pos] : ctx->pos[ctx->cur];
+    if (vel4) *vel4 = bh ? ctx->vel2[ctx->bh_va] : ctx->vel;
+    if (acc4) *acc4 = bh ? ctx->acc2[ctx->bh_va] : ctx->acc;
+    return NBODY_OK;
+}
+
+int nbody_device_order(nbody_ctx *ctx, void **ids) {
+    if (!ctx || !ids) return NBODY_ERR_ARG;
+    *ids = (ctx->mode == NBODY_MODE_BH && ctx->ids_valid) ? static_cast<void *>(ctx->ids[ctx->bh_va]) : nullptr;
+    return NBODY_OK;
+}
+
+int nbody_bh_keys_device(nbody_ctx *ctx, const void *pos_mass4, int64_t n, void *keys_out, void *box_out) {
+    if (!ctx || !pos_mass4 || n <= 0 || !aligned16(pos_mass4)) return NBODY_ERR_ARG;
+    DeviceGuard dg(ctx->device);
+    int rc = ensure_workspace(ctx, n);
+    if (rc != NBODY_OK) return rc;
+    nbody::BHWorkspace &w = ctx->ws;
+    const float4 *p = static_cast<const float4 *>(pos_mass4);
+    NB_CK(ctx, nbody::bh_bbox(p, n, w, ctx->stream, ctx->timer));
+    NB_CK(ctx, nbody::bh_keys(p, n, w, ctx->stream, ctx->timer));
+    if (keys_out)
+        NB_CK(ctx, cudaMemcpyAsync(keys_out, w.keys[0], sizeof(uint64_t) * static_cast<size_t>(n),
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+    if (box_out) NB_CK(ctx, cudaMemcpyAsync(box_out, w.box, sizeof(float) * 6, cudaMemcpyDeviceToDevice, ctx->stream));
+    return NBODY_OK;
+}
+
+int nbody_sort_pairs_device(nbody_ctx *ctx, void *keys, void *vals, int64_t n) {
+    if (!ctx || !keys || !vals || n < 0) return NBODY_ERR_ARG;
+    if (n <= 1) return NBODY_OK;
+    DeviceGuard dg(ctx->device);
+    int rc = ensure_workspace(ctx, n);
+    if (rc != NBODY_OK) return rc;
+    nbody::BHWorkspace &w = ctx->ws;
+    int alt = 0;
+    NB_CK(ctx, nbody::sort_pairs(static_cast<uint64_t *>(keys), static_cast<uint32_t *>(vals), w.keys[1], w.vals[1], n,
+                                 w.sort_scratch, ctx->stream, ctx->status, &alt));
+    if (alt) {
+        NB_CK(ctx, cudaMemcpyAsync(keys, w.keys[1], sizeof(uint64_t) * static_cast<size_t>(n), cudaMemcpyDeviceToDevice,
+                                   ctx->stream));
+        NB_CK(ctx, cudaMemcpyAsync(vals, w.vals[1], sizeof(uint32_t) * static_cast<size_t>(n), cudaMemcpyDeviceToDevice,
+                                   ctx->stream));
+    }
+    return NBODY_OK;
+}
+
+int nbody_bh_forces_device(nbody_ctx *ctx, const void *pos_mass4, void *force4, int64_t n) {
+    if (!ctx || !pos_mass4 || !force4 || n <= 0 || !aligned16(pos_mass4) || !aligned16(force4))
+        return NBODY_ERR_ARG;
+    DeviceGuard dg(ctx->device);
+    int rc = ensure_workspace(ctx, n);
+    if (rc != NBODY_OK) return rc;
+    if (ctx->dev_cap < n) {
+        NB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->dev_pos);
+        cudaFree(ctx->dev_ids);
+        ctx->dev_pos = nullptr;
+        ctx->dev_ids = nullptr;
+        ctx->dev_cap = 0;
+        NB_CK(ctx, cudaMalloc(&ctx->dev_pos, sizeof(float4) * static_cast<size_t>(n)));
+        NB_CK(ctx, cudaMalloc(&ctx->dev_ids, sizeof(int) * static_cast<size_t>(n)));
+        ctx->dev_cap = n;
+    }
+    nbody::BHWorkspace &w = ctx->ws;
+    const float4 *p = static_cast<const float4 *>(pos_mass4);
+    nbody::StageTimer *tm = ctx->timer;
+    NB_CK(ctx, nbody::bh_bbox(p, n, w, ctx->stream, tm));
+    NB_CK(ctx, nbody::bh_keys(p, n, w, ctx->stream, tm));
+    NB_CK(ctx, nbody::bh_sort(n, w, ctx->stream, ctx->status, tm));
+    NB_CK(ctx, nbody::bh_gather(n, w, p, nullptr, nullptr, nullptr, ctx->dev_pos, nullptr, nullptr, ctx->dev_ids,
+                                ctx->stream, ctx->status, tm));
+    NB_CK(ctx, nbody::bh_build(ctx->dev_pos, n, w, ctx->stream, ctx->status, tm));
+    NB_CK(ctx, nbody::bh_traverse(ctx->dev_pos, n, w, ctx->eps2, ctx->theta2, 0.f, nullptr, nullptr, nullptr,
+                                  static_cast<float4 *>(force4), ctx->dev_ids, ctx->stream, tm));
+    return NBODY_OK;
+}
+
+int nbody_bh_tree_export(nbody_ctx *ctx, float *records_host, int64_t cap, int64_t *count, float *box_host) {
+    if (!ctx || !count) return NBODY_ERR_ARG;
+    *count = 0;
+    if (!ctx->ws_mem) return NBODY_ERR_STATE;
+    DeviceGuard dg(ctx->device);
+    const nbody::BHWorkspace &w = ctx->ws;
+    uint32_t m = 0;
+    NB_CK(ctx, cudaMemcpyAsync(&m, w.P + w.n, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    NB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    *count = m;
+    if (box_host) NB_CK(ctx, cudaMemcpy(box_host, w.box, sizeof(float) * 6, cudaMemcpyDeviceToHost));
+    if (records_host && cap > 0) {
+        const int64_t k = std::min<int64_t>(cap, m);
+        NB_CK(ctx, cudaMemcpy(records_host, w.nodes, sizeof(nbody::BHNode) * static_cast<size_t>(k),
+                              cudaMemcpyDeviceToHost));
+    }
     return NBODY_OK;
 }
 
@@ -374,6 +569,13 @@ const char *nbody_stage_name(int stage) {
     switch (stage) {
         case nbody::kStagePPForce: return "pp_force";
         case nbody::kStagePack: return "pack";
+        case nbody::kStageBBox: return "bh_bbox";
+        case nbody::kStageMorton: return "bh_morton";
+        case nbody::kStageSort: return "bh_sort";
+        case nbody::kStageGather: return "bh_gather";
+        case nbody::kStageBuild: return "bh_build";
+        case nbody::kStageUpsweep: return "bh_upsweep";
+        case nbody::kStageTraverse: return "bh_traverse";
         default: return "";
     }
 }

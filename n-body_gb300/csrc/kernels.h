@@ -18,7 +18,18 @@ struct Integrate {
 
 // Optional per-stage timing: when set, launchers record a CUDA event pair
 // around each kernel on the launch stream (see capi.cu: nbody_profile_*).
-enum Stage { kStagePPForce = 0, kStagePack, kStageCount };
+enum Stage {
+    kStagePPForce = 0,
+    kStagePack,
+    kStageBBox,
+    kStageMorton,
+    kStageSort,
+    kStageGather,
+    kStageBuild,
+    kStageUpsweep,
+    kStageTraverse,
+    kStageCount
+};
 
 struct StageTimer {
     virtual ~StageTimer() = default;

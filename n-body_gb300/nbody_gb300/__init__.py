@@ -58,6 +58,11 @@ SIGNATURES = {
     "nbody_stage_name": (ctypes.c_char_p, [_i]),
     "nbody_stage_count": (_i, []),
     "nbody_pp_forces_noalloc": (_i, [_vp, _vp, _i64, _f, _vp, _ip]),
+    "nbody_device_order": (_i, [_vp, ctypes.POINTER(_vp)]),
+    "nbody_bh_keys_device": (_i, [_vp, _vp, _i64, _vp, _vp]),
+    "nbody_sort_pairs_device": (_i, [_vp, _vp, _vp, _i64]),
+    "nbody_bh_forces_device": (_i, [_vp, _vp, _vp, _i64]),
+    "nbody_bh_tree_export": (_i, [_vp, _vp, _i64, ctypes.POINTER(_i64), _vp]),
 }
 
 
@@ -235,6 +240,41 @@ class ParticleSolverCUDA:
         cnt = (ctypes.c_int * k)()
         self._check(lib().nbody_profile_read(self._ctx, ms, cnt, k), "nbody_profile_read")
         return {lib().nbody_stage_name(i).decode(): (ms[i], cnt[i]) for i in range(k) if cnt[i]}
+
+    def device_order(self):
+        p = ctypes.c_void_p()
+        self._check(lib().nbody_device_order(self._ctx, ctypes.byref(p)), "nbody_device_order")
+        return p.value
+
+    def bh_keys_device(self, pos_mass, keys_out, box_out=None, n: int | None = None) -> None:
+        n = self.n if n is None else int(n)
+        self._check(lib().nbody_bh_keys_device(self._ctx, _ptr(pos_mass), n, _ptr(keys_out), _ptr(box_out)),
+                    "nbody_bh_keys_device")
+
+    def sort_pairs_device(self, keys, vals, n: int | None = None) -> None:
+        n = self.n if n is None else int(n)
+        self._check(lib().nbody_sort_pairs_device(self._ctx, _ptr(keys), _ptr(vals), n), "nbody_sort_pairs_device")
+
+    def bh_forces_device(self, pos_mass, force, n: int | None = None) -> None:
+        n = self.n if n is None else int(n)
+        self._check(lib().nbody_bh_forces_device(self._ctx, _ptr(pos_mass), _ptr(force), n),
+                    "nbody_bh_forces_device")
+
+    def bh_tree(self):
+        """Pre-order records of the last Barnes-Hut build and the root box.
+
+        Returns (cm, meta, box): cm float32 (M, 4) centre of mass + mass;
+        meta int32 (M, 4): side^2 bits (float, -1 for leaves), next, first
+        body, leaf body count; box float32 (6,)."""
+        count = ctypes.c_int64()
+        self._check(lib().nbody_bh_tree_export(self._ctx, None, 0, ctypes.byref(count), None), "nbody_bh_tree_export")
+        m = count.value
+        rec = np.zeros((max(m, 1), 8), np.float32)
+        box = np.zeros(6, np.float32)
+        self._check(lib().nbody_bh_tree_export(self._ctx, _ptr(rec), m, ctypes.byref(count), _ptr(box)),
+                    "nbody_bh_tree_export")
+        rec = rec[:m]
+        return rec[:, :4].copy(), rec[:, 4:].view(np.int32).copy(), box
 
     def close(self) -> None:
         if self._ctx:
