@@ -4,6 +4,11 @@
 
 Workloads (seeded synthetic inputs with the shapes the configurations name;
 no public dataset is involved):
+  bh (default): Barnes-Hut, N = 2^20 equal-mass Plummer sphere (a = 100,
+       truncated at 20a, velocities from the Plummer distribution function),
+       theta = 0.5, eps^2 = 40, dt = 0.0035 (the reference's -v 6 path).
+       Metric: body-steps/s. The line also carries a "pp" object with the
+       direct-sum workload measured the same way.
   pp : direct sum, N = 16,384 bodies uniform in a ball of radius 100, masses
        U[1, 10), v = 0, dt = 0.0035, eps^2 = 40 (the reference's -v 2 path).
        Metric: interactions/s (N^2 per step, 20 flop each by convention).
@@ -41,6 +46,15 @@ import numpy as np  # noqa: E402
 
 METRIC = "PP interactions/s (%FP32 peak), BH body-steps/s; served sims/s + p99 vs plain"
 PP_N, PP_DT, PP_EPS2 = 16384, 0.0035, 40.0
+BH_N, BH_DT, BH_EPS2, BH_THETA2 = 1 << 20, 0.0035, 40.0, 0.25
+# Algorithmic bytes per body per step of the HBM-bound Barnes-Hut stages:
+# bbox reads pos (16); keys read pos, write key + index (16 + 12); the sort reads
+# keys once for the histograms (8) and moves key + index in and out in 8 passes
+# (8 x 24); the gather reads index, pos, vel, acc, id and writes them (4 + 52 + 52);
+# the build reads two neighbour keys per body and writes a 32-byte record (16 + 32);
+# the upsweep reads a position and writes a partial sum per node (16 + 32).
+BH_STAGE_BYTES = {"bh_bbox": 16, "bh_morton": 28, "bh_sort": 200, "bh_gather": 108, "bh_build": 48,
+                  "bh_upsweep": 48}
 FLOP_PER_INTERACTION = 20
 L2_FLUSH_BYTES = 256 << 20
 
@@ -269,7 +283,145 @@ def bench_pp(args, world, rank, local, dist):
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_pp()
     solver.close()
+    torch.cuda.set_stream(torch.cuda.default_stream())
     return line
+
+
+# ------------------------------------------------------------------ BH (ours)
+def bench_bh(args, world, rank, local, dist):
+    import torch
+
+    import nbody_gb300 as nb
+    from nbody_gb300 import initializers as I
+
+    torch.cuda.set_device(local)
+    n = BH_N
+    pos, vel, mass = I.plummer(n, a=100.0, seed=12345 + rank)
+    system = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+    solver = nb.ParticleSolverCUDA(BH_DT, BH_EPS2, n, mode="bh", theta2=BH_THETA2, device=local)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    solver.set_stream(stream.cuda_stream)
+    solver.upload(system)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def timed_steps(k):
+        evs = []
+        for _ in range(k):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            solver.step(1)
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in evs)
+
+    timed_steps(max(3, args.warmup))
+    solver.sync()
+    sampler = ClockSampler(local)
+    sampler.start()
+    t_end = time.time() + 1.5
+    while time.time() < t_end:
+        timed_steps(5)
+    barrier(dist)
+    torch.cuda.synchronize()
+    ms = timed_steps(args.steps)
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    solver.sync()
+    ms = max_over_ranks(dist, ms)
+    sec = ms / 1e3
+    value = float(n) * args.steps * world / sec
+
+    # per-stage CUDA events on the launch stream (a separate pass)
+    solver.profile_enable(True)
+    timed_steps(args.steps)
+    prof = solver.profile_read()
+    solver.profile_enable(False)
+    # work of the traversal (pairwise evaluations), counted in one more pass
+    solver.bh_counters(True)
+    timed_steps(1)
+    pairs, visits = solver.bh_counters(False)
+    pk = peaks()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32 = fp32_peak_tflops(sms, float(pk.get("sm_max_mhz", 2070.0)))
+    t_ms, t_cnt = prof.get("bh_traverse", (0.0, 1))
+    t_launch = t_ms / 1e3 / max(1, t_cnt)
+    achieved = FLOP_PER_INTERACTION * pairs / t_launch / 1e12
+    stages = {}
+    for name, (sms_ms, cnt) in prof.items():
+        per = sms_ms / max(1, cnt)
+        st = {"ms": round(per, 4), "share": round(sms_ms / max(1e-9, sum(v[0] for v in prof.values())), 4)}
+        if name in BH_STAGE_BYTES:
+            gbs = BH_STAGE_BYTES[name] * n / (per / 1e3) / 1e9
+            st.update({"bytes_per_body": BH_STAGE_BYTES[name], "achieved_gbs": round(gbs, 1),
+                       "hbm_frac": round(gbs / pk["hbm_gbs"], 4)})
+        stages[name] = st
+    roofline = {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(fp32, 3), "unit": "TFLOP/s",
+                "frac": round(achieved / fp32, 4), "traffic": profile_traffic("bh_traverse"),
+                "kernel": "traverse_kernel", "kernel_ms_per_launch": round(t_launch * 1e3, 4),
+                "work": {"pair_evaluations_per_step": pairs, "per_body": round(pairs / n, 1),
+                         "warp_record_visits_per_step": visits,
+                         "lane_efficiency": round(pairs / max(1, visits * 32), 4)},
+                "peak_note": f"nominal FP32 FMA peak ({sms} SMs x 128 lanes x 2 flop x {pk.get('sm_max_mhz')} MHz, "
+                             f"{pk['source']} peaks file); 20 flop per pairwise evaluation, as for the direct sum. "
+                             f"The traversal is latency/issue-bound; the other stages are graded against "
+                             f"{pk['hbm_gbs']} GB/s HBM ({pk['source']}) in stages.",
+                "stages": stages}
+
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    hsys = nb.ParticleSystem(pin(pos.copy()), pin(vel.copy()), mass)
+    hsys.masses = pin(hsys.masses)
+    hsys.forces = pin(hsys.forces)
+    hsys.accelerations = pin(hsys.accelerations)
+    for _ in range(2):
+        solver.update_particle_positions(hsys)
+    torch.cuda.synchronize()
+    barrier(dist)
+    e2e_steps = max(1, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        solver.update_particle_positions(hsys)
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e = {"value": float(n) * e2e_steps * world / e2e_s, "unit": "body-steps/s", "h2d_bytes_per_step": 4 * 16 * n,
+           "d2h_bytes_per_step": 4 * 16 * n, "ms_per_step": round(e2e_s * 1e3 / e2e_steps, 3), "steps": e2e_steps,
+           "api": "nbody_update_host (ParticleSolver::updateParticlePositions)"}
+    launches_per_step = 23
+    line = {"metric": METRIC, "component": "BH body-steps/s", "value": value, "unit": "body-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "Barnes-Hut, N=1048576 equal-mass Plummer sphere a=100 (truncated at 20a, "
+                                   "velocities from the Plummer DF), theta=0.5, eps2=40, dt=0.0035 "
+                                   "(reference -v 6 path)", "n_bodies": n, "parallelism": "replicas",
+                       "l2": "flushed between steps (256 MiB write, outside the event pair)"},
+            "clocks": clocks, "roofline": roofline, "e2e": e2e, "gpu_launches": launches_per_step * args.steps}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_bh()
+    solver.close()
+    torch.cuda.set_stream(torch.cuda.default_stream())
+    return line
+
+
+def cpu_baseline_bh(budget_s: float = 15.0):
+    import pyoracle
+    from nbody_gb300 import initializers as I
+
+    pyoracle.build(reference=False)
+    threads = cpu_threads()
+    pos, vel, mass = I.plummer(BH_N, a=100.0, seed=12345)
+    acc = np.zeros_like(pos)
+    r = pyoracle.bh_run(pos, vel, acc, mass, BH_DT, BH_EPS2, 1, theta2=BH_THETA2, threads=threads, patched=True)
+    t1 = r[4]["seconds"]
+    steps = max(1, min(10, int(budget_s / max(t1, 1e-3))))
+    r = pyoracle.bh_run(pos, vel, acc, mass, BH_DT, BH_EPS2, steps, theta2=BH_THETA2, threads=threads, patched=True)
+    return {"value": float(BH_N) * steps / r[4]["seconds"], "unit": "body-steps/s", "cores": threads,
+            "kind": "port", "sample": f"{steps} full steps of the N=1048576 Plummer workload (-v 6 restated: "
+                                      f"OpenMP tasks, integer node links, subtree regions sized from their "
+                                      f"body counts; the reference's own -v 6 overflows its fixed regions on "
+                                      f"this input), {threads} threads"}
 
 
 def cpu_kind():
@@ -314,34 +466,58 @@ def bench_reference(args, world, rank):
 
     pyoracle.build(reference=False)
     threads = cpu_threads()
-    pos, vel, mass = I.uniform_ball(PP_N, seed=12345)
-    for _ in range(args.warmup):
-        cpu_pp_step_seconds(pos, vel, mass, 1, threads)
-    # each step is one full -v 2 step; the count is bounded to keep the run within minutes
-    t1 = cpu_pp_step_seconds(pos, vel, mass, 1, threads)
-    steps = max(1, min(args.steps, int(120.0 / max(t1, 1e-3))))
-    secs = cpu_pp_step_seconds(pos, vel, mass, steps, threads)
-    value = float(PP_N) * PP_N * steps / secs
-    kind = cpu_kind()
-    return {"impl": "reference", "metric": METRIC, "component": "PP interactions/s", "value": value,
-            "unit": "interactions/s", "n_gpus": world, "steps": steps, "warmup": args.warmup,
-            "ms_per_step": secs * 1e3 / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "direct-sum PP, N=16384 uniform ball R=100, m~U[1,10), v=0, dt=0.0035, "
-                                   "eps2=40 (reference -v 2 path)", "n_bodies": PP_N, "parallelism": "host cores"},
-            "cpu_baseline": {"value": value, "unit": "interactions/s", "cores": threads, "kind": kind,
-                             "sample": f"{steps} full steps (-v 2 OpenMP, {threads} threads)"},
-            "e2e": {"value": value, "unit": "interactions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if args.workload == "pp":
+        pos, vel, mass = I.uniform_ball(PP_N, seed=12345)
+        for _ in range(args.warmup):
+            cpu_pp_step_seconds(pos, vel, mass, 1, threads)
+        # each step is one full -v 2 step; the count is bounded to keep the run within minutes
+        t1 = cpu_pp_step_seconds(pos, vel, mass, 1, threads)
+        steps = max(1, min(args.steps, int(120.0 / max(t1, 1e-3))))
+        secs = cpu_pp_step_seconds(pos, vel, mass, steps, threads)
+        value = float(PP_N) * PP_N * steps / secs
+        kind = cpu_kind()
+        unit, comp = "interactions/s", "PP interactions/s"
+        workload = ("direct-sum PP, N=16384 uniform ball R=100, m~U[1,10), v=0, dt=0.0035, eps2=40 "
+                    "(reference -v 2 path)")
+        sample = f"{steps} full steps (-v 2 OpenMP, {threads} threads)"
+        n = PP_N
+    else:
+        pos, vel, mass = I.plummer(BH_N, a=100.0, seed=12345)
+        acc = np.zeros_like(pos)
+        # warm-up, then a bounded number of full -v 6 steps (each a few seconds)
+        r = pyoracle.bh_run(pos, vel, acc, mass, BH_DT, BH_EPS2, 1, theta2=BH_THETA2, threads=threads,
+                            patched=True)
+        t1 = r[4]["seconds"]
+        steps = max(1, min(args.steps, int(120.0 / max(t1, 1e-3))))
+        r = pyoracle.bh_run(pos, vel, acc, mass, BH_DT, BH_EPS2, steps, theta2=BH_THETA2, threads=threads,
+                            patched=True)
+        secs = r[4]["seconds"]
+        value = float(BH_N) * steps / secs
+        kind = "port"
+        unit, comp = "body-steps/s", "BH body-steps/s"
+        workload = ("Barnes-Hut, N=1048576 equal-mass Plummer sphere a=100 (truncated at 20a, velocities from "
+                    "the Plummer DF), theta=0.5, eps2=40, dt=0.0035 (reference -v 6 path)")
+        sample = (f"{steps} full steps (-v 6 restated with integer node links and subtree regions sized from "
+                  f"their body counts; the reference's own -v 6 overflows its fixed regions on this input), "
+                  f"{threads} threads")
+        n = BH_N
+    return {"impl": "reference", "metric": METRIC, "component": comp, "value": value, "unit": unit,
+            "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload, "n_bodies": n, "parallelism": "host cores"},
+            "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
-    ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", choices=["pp"], default="pp")
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", choices=["bh", "pp"], default="bh")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-pp", action="store_true", help="leave the nested direct-sum measurement out")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_env()
@@ -356,7 +532,17 @@ def main():
     if not os.path.exists(nbody_gb300.LIB_PATH):
         nbuild.build()
     dist = init_dist(world, local)
-    line = bench_pp(args, world, rank, local, dist)
+    if args.workload == "pp":
+        line = bench_pp(args, world, rank, local, dist)
+    else:
+        line = bench_bh(args, world, rank, local, dist)
+        if not args.no_pp:
+            pp_args = argparse.Namespace(**vars(args))
+            pp_args.steps = 100
+            pp = bench_pp(pp_args, world, rank, local, dist)
+            line["pp"] = {k: pp[k] for k in ("component", "value", "unit", "steps", "ms_per_step", "roofline",
+                                             "e2e", "clocks", "gpu_launches", "config", "cpu_baseline")
+                          if k in pp}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

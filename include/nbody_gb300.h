@@ -136,6 +136,13 @@ int nbody_sort_pairs_device(nbody_ctx *ctx, void *keys, void *vals, int64_t n);
 int nbody_bh_forces_device(nbody_ctx *ctx, const void *pos_mass4, void *force4, int64_t n);
 int nbody_bh_tree_export(nbody_ctx *ctx, float *records_host, int64_t cap, int64_t *count, float *box_host);
 
+/* Barnes-Hut work counters, for measurement: returns (and clears) the number
+ * of pairwise force evaluations and of tree records visited by warps since
+ * the last call, then enables (enable != 0) or disables counting for later
+ * traversals. Counting uses a separate traversal variant; leave it off when
+ * timing. */
+int nbody_bh_counters(nbody_ctx *ctx, int enable, int64_t *pair_evaluations, int64_t *warp_visits);
+
 /* Per-stage timing. While enabled, every kernel stage launched by this
  * context is bracketed by a CUDA event pair on its launch stream.
  * nbody_profile_read waits for them, writes the summed milliseconds and launch

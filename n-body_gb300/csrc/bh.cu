@@ -335,12 +335,17 @@ __global__ void upsweep_kernel(int64_t n, const float4 *__restrict__ pos, Binary
 // the record's `next`. The warp descends (i + 1) if any lane opened the
 // record, otherwise it jumps to the smallest `skip` of its lanes. Every lane
 // therefore sees exactly the records its own reference walk would accept.
+// COUNT adds up (per warp, one atomic each) the pairwise force evaluations
+// and the records the warp visited; used for measurement only.
+template <bool COUNT>
 __global__ void __launch_bounds__(256) traverse_kernel(const BHNode *__restrict__ nodes,
                                                        const uint32_t *__restrict__ node_total,
                                                        const float4 *__restrict__ pos, int64_t n, float eps2,
                                                        float theta2, float dt, float4 *__restrict__ pos_out,
                                                        float4 *__restrict__ vel, float4 *__restrict__ acc,
-                                                       float4 *__restrict__ force_out, const int *__restrict__ ids) {
+                                                       float4 *__restrict__ force_out, const int *__restrict__ ids,
+                                                       unsigned long long *__restrict__ counters) {
+    unsigned long long n_pairs = 0, n_visits = 0;
     const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const bool valid = b < n;
     const int m_nodes = static_cast<int>(*node_total);
@@ -364,6 +369,7 @@ __global__ void __launch_bounds__(256) traverse_kernel(const BHNode *__restrict_
                         const float ex = o.x - me.x, ey = o.y - me.y, ez = o.z - me.z;
                         const float e2 = __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
                         if (o.w > 0.f && e2 > 0.f) {
+                            if (COUNT) ++n_pairs;
                             const float inv = rsqrt_ftz(e2 + eps2);
                             const float w = o.w * inv * inv * inv;
                             fx = fmaf(ex, w, fx);
@@ -372,6 +378,7 @@ __global__ void __launch_bounds__(256) traverse_kernel(const BHNode *__restrict_
                         }
                     }
                 } else if (cm.w > 0.f && d2 > 0.f) {
+                    if (COUNT) ++n_pairs;
                     const float inv = rsqrt_ftz(d2 + eps2);
                     const float w = cm.w * inv * inv * inv;
                     fx = fmaf(dx, w, fx);
@@ -383,6 +390,7 @@ __global__ void __launch_bounds__(256) traverse_kernel(const BHNode *__restrict_
                 open = true;
             }
         }
+        if (COUNT) ++n_visits;
         if (__any_sync(0xffffffffu, open)) {
             ++i;
         } else {
@@ -390,6 +398,14 @@ __global__ void __launch_bounds__(256) traverse_kernel(const BHNode *__restrict_
             // (at most m_nodes iterations) whatever the records hold.
             const int nx = static_cast<int>(__reduce_min_sync(0xffffffffu, static_cast<unsigned>(skip)));
             i = nx > i ? nx : i + 1;
+        }
+    }
+    if (COUNT) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) n_pairs += __shfl_down_sync(0xffffffffu, n_pairs, off);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&counters[0], n_pairs);
+            atomicAdd(&counters[1], n_visits);
         }
     }
     if (!valid) return;
@@ -567,6 +583,8 @@ size_t bh_workspace_layout(int64_t n, void *base, BHWorkspace *w) {
     w->P = static_cast<uint32_t *>(take(sizeof(uint32_t) * (nn + 1)));
     w->scan_sums = static_cast<uint32_t *>(take(sizeof(uint32_t) * static_cast<size_t>(tiles + 1)));
     w->nodes = static_cast<BHNode *>(take(sizeof(BHNode) * 2 * nn));
+    w->counter_mem = static_cast<unsigned long long *>(take(sizeof(unsigned long long) * 2));
+    w->counters = nullptr;
     w->node_count_host = 0;
     return (off + 255) & ~static_cast<size_t>(255);
 }
@@ -646,8 +664,12 @@ cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &
                         cudaStream_t st, StageTimer *timer) {
     if (timer) timer->begin(kStageTraverse, st);
     // The record count P[n] stays on the device; the kernel reads it.
-    traverse_kernel<<<grid_for(n, 256), 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel,
-                                                      acc, force_out, ids);
+    if (w.counters)
+        traverse_kernel<true><<<grid_for(n, 256), 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
+                                                                pos_out, vel, acc, force_out, ids, w.counters);
+    else
+        traverse_kernel<false><<<grid_for(n, 256), 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
+                                                                 pos_out, vel, acc, force_out, ids, nullptr);
     if (timer) timer->end(kStageTraverse, st);
     return cudaGetLastError();
 }

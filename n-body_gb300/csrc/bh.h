@@ -42,6 +42,10 @@ struct BHWorkspace {
     uint32_t *P = nullptr;  // n + 1 entries; P[n] = record count
     uint32_t *scan_sums = nullptr;
     BHNode *nodes = nullptr;  // up to 2n records
+    // Traversal counters (pairwise evaluations, warp record visits): the
+    // traversal counts into `counters` when it is set (= counter_mem).
+    unsigned long long *counter_mem = nullptr;
+    unsigned long long *counters = nullptr;
     int64_t node_count_host = 0;
 };
 

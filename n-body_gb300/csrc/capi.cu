@@ -194,7 +194,9 @@ int ensure_workspace(nbody_ctx *ctx, int64_t n) {
     NB_CK(ctx, cudaMalloc(&ctx->ws_mem, bytes));
     NB_CK(ctx, cudaMemsetAsync(ctx->ws_mem, 0, bytes, ctx->stream));
     ctx->ws_bytes = bytes;
+    const bool counting = ctx->ws.counters != nullptr;
     nbody::bh_workspace_layout(n, ctx->ws_mem, &ctx->ws);
+    if (counting) ctx->ws.counters = ctx->ws.counter_mem;
     return NBODY_OK;
 }
 
@@ -605,6 +607,21 @@ int nbody_profile_read(nbody_ctx *ctx, double *ms, int *launches, int nstages) {
     if (!ctx->timer) return NBODY_OK;
     DeviceGuard dg(ctx->device);
     NB_CK(ctx, ctx->timer->read(ms, launches, nstages));
+    return NBODY_OK;
+}
+
+int nbody_bh_counters(nbody_ctx *ctx, int enable, int64_t *pair_evaluations, int64_t *warp_visits) {
+    if (!ctx) return NBODY_ERR_ARG;
+    DeviceGuard dg(ctx->device);
+    int rc = ensure_workspace(ctx, ctx->n);
+    if (rc != NBODY_OK) return rc;
+    unsigned long long h[2] = {0ull, 0ull};
+    NB_CK(ctx, cudaMemcpyAsync(h, ctx->ws.counter_mem, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    NB_CK(ctx, cudaMemsetAsync(ctx->ws.counter_mem, 0, sizeof(h), ctx->stream));
+    NB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (pair_evaluations) *pair_evaluations = static_cast<int64_t>(h[0]);
+    if (warp_visits) *warp_visits = static_cast<int64_t>(h[1]);
+    ctx->ws.counters = enable ? ctx->ws.counter_mem : nullptr;
     return NBODY_OK;
 }
 

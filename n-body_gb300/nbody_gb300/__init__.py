@@ -63,6 +63,7 @@ SIGNATURES = {
     "nbody_sort_pairs_device": (_i, [_vp, _vp, _vp, _i64]),
     "nbody_bh_forces_device": (_i, [_vp, _vp, _vp, _i64]),
     "nbody_bh_tree_export": (_i, [_vp, _vp, _i64, ctypes.POINTER(_i64), _vp]),
+    "nbody_bh_counters": (_i, [_vp, _i, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
 }
 
 
@@ -275,6 +276,13 @@ class ParticleSolverCUDA:
                     "nbody_bh_tree_export")
         rec = rec[:m]
         return rec[:, :4].copy(), rec[:, 4:].view(np.int32).copy(), box
+
+    def bh_counters(self, enable: bool):
+        """(pair evaluations, warp record visits) since the last call; then counting on/off."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._check(lib().nbody_bh_counters(self._ctx, int(enable), ctypes.byref(a), ctypes.byref(b)),
+                    "nbody_bh_counters")
+        return a.value, b.value
 
     def close(self) -> None:
         if self._ctx:
