@@ -46,6 +46,19 @@ extern "C" {
 #define NBODY_MODE_PP 0 /* direct sum, reference -v 2 (CPU) / -v 3, -v 4 (GLSL)   */
 #define NBODY_MODE_BH 1 /* Barnes-Hut, reference -v 6 (CPU) / -v 7 (GLSL)         */
 
+/* 63-bit keys that order bodies for the Barnes-Hut tree (21 bits per axis,
+ * x highest in each bit triple, over the per-step root box):
+ * NBODY_KEYS_OCTREE (default): the reference's own octree descent taken 21
+ *   levels deep -- per level and axis centre = min + (max - min) / 2 in FP32,
+ *   upper half unless pos < centre (Octree::getNextNode / Octree::subdivide,
+ *   src/Octree/Octree.cpp:148-231). Cells are then exactly the reference's.
+ * NBODY_KEYS_MORTON: the reference's GLSL Morton quantisation extended to 21
+ *   bits, q = uint(clamp((p - min) / max(max - min, 1e-6) * 2^21, 0, 2^21 - 1))
+ *   (src/shaders/ComputeShaders/morton.glsl:37-75). The two differ only for
+ *   bodies within rounding of a cell boundary. */
+#define NBODY_KEYS_OCTREE 0
+#define NBODY_KEYS_MORTON 1
+
 typedef struct nbody_ctx nbody_ctx;
 
 /* Human-readable name of a status code. */
@@ -110,13 +123,15 @@ int nbody_pp_step_device(nbody_ctx *ctx, const void *pos_in, void *pos_out, void
  * thread, j-slices and CTAs. For tests and tuning reports. */
 int nbody_pp_config(nbody_ctx *ctx, int64_t n, int *bodies_per_thread, int *slices, int *ctas);
 
+/* Selects the key used to build the Barnes-Hut tree (NBODY_KEYS_*). */
+int nbody_set_key_mode(nbody_ctx *ctx, int mode);
+
 /* Barnes-Hut pieces on device buffers (context's stream and workspace).
  *
  * nbody_bh_keys_device: the root box of n bodies (min xyz, max xyz; the
  * reference's seeds, src/Octree/ParallelOctreeCPU.cpp:76-118) into box_out
- * (6 floats, device) and their 63-bit Morton keys into keys_out (uint64,
- * device): 21 bits per axis, x highest in each triple, quantised as
- * src/shaders/ComputeShaders/morton.glsl:49-75 does with 2^21 cells per axis.
+ * (6 floats, device) and their 63-bit keys of the context's key mode
+ * (NBODY_KEYS_*) into keys_out (uint64, device).
  *
  * nbody_sort_pairs_device: sorts (uint64 key, uint32 value) pairs by key in
  * place, stably -- replaces src/shaders/ComputeShaders/bitonicSort.glsl:23-50.

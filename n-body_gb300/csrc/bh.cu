@@ -98,17 +98,39 @@ __global__ void bbox_kernel(const float4 *__restrict__ pos, int64_t n, float *__
         last = atomicAdd(counter, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        float r[6] = {FLT_MAX, FLT_MAX, FLT_MAX, FLT_MIN, FLT_MIN, FLT_MIN};
-        for (unsigned b = 0; b < gridDim.x; ++b)
+    if (!last) return;
+    // Last block: every thread folds a strided share of the partials, then
+    // the block reduces as above.
+    __threadfence();
+    float r[6] = {FLT_MAX, FLT_MAX, FLT_MAX, FLT_MIN, FLT_MIN, FLT_MIN};
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+        for (int a = 0; a < 3; ++a) {
+            const float lo = __ldcg(&partial[b * 6 + a]);
+            const float hi = __ldcg(&partial[b * 6 + 3 + a]);
+            if (lo < r[a]) r[a] = lo;
+            if (hi > r[3 + a]) r[3 + a] = hi;
+        }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float o1 = __shfl_down_sync(0xffffffffu, r[a], off);
+            const float o2 = __shfl_down_sync(0xffffffffu, r[3 + a], off);
+            if (o1 < r[a]) r[a] = o1;
+            if (o2 > r[3 + a]) r[3 + a] = o2;
+        }
+    }
+    __syncthreads();
+    if (lane == 0)
+        for (int a = 0; a < 6; ++a) wm[warp][a] = r[a];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < nw; ++w)
             for (int a = 0; a < 3; ++a) {
-                const float lo = __ldcg(&partial[b * 6 + a]);
-                const float hi = __ldcg(&partial[b * 6 + 3 + a]);
-                if (lo < r[a]) r[a] = lo;
-                if (hi > r[3 + a]) r[3 + a] = hi;
+                if (wm[w][a] < wm[0][a]) wm[0][a] = wm[w][a];
+                if (wm[w][3 + a] > wm[0][3 + a]) wm[0][3 + a] = wm[w][3 + a];
             }
-        for (int a = 0; a < 6; ++a) box[a] = r[a];
+        for (int a = 0; a < 6; ++a) box[a] = wm[0][a];
         *counter = 0u;
     }
 }
@@ -136,15 +158,46 @@ __device__ __forceinline__ uint32_t quantize21(float p, float lo, float hi) {
     return __float2uint_rz(g);
 }
 
+// The reference's own octree descent (Octree::getNextNode with the child
+// boxes of Octree::subdivide, src/Octree/Octree.cpp:148-231) taken 21 levels
+// deep from the root box: per level and axis, centre = min + (max - min) / 2 in
+// FP32 and the body goes to the upper half unless pos < centre. The key bits
+// are the halves taken (1 = upper), x highest in each triple, so cells of
+// this key are exactly the reference's cells and body membership is decided
+// by the same comparisons.
+__device__ __forceinline__ uint64_t octree_key(float px, float py, float pz, const float *__restrict__ box) {
+    float mn[3] = {box[0], box[1], box[2]};
+    float mx[3] = {box[3], box[4], box[5]};
+    const float p[3] = {px, py, pz};
+    uint64_t key = 0;
+    for (int l = 0; l < 21; ++l) {
+        uint32_t digit = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float c = __fadd_rn(mn[a], __fmul_rn(__fsub_rn(mx[a], mn[a]), 0.5f));
+            const bool upper = !(p[a] < c);
+            if (upper) mn[a] = c; else mx[a] = c;
+            digit |= static_cast<uint32_t>(upper) << (2 - a);
+        }
+        key = (key << 3) | digit;
+    }
+    return key;
+}
+
+template <int MODE>
 __global__ void morton_kernel(const float4 *__restrict__ pos, int64_t n, const float *__restrict__ box,
                               uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 p = pos[i];
-    const uint64_t qx = quantize21(p.x, box[0], box[3]);
-    const uint64_t qy = quantize21(p.y, box[1], box[4]);
-    const uint64_t qz = quantize21(p.z, box[2], box[5]);
-    keys[i] = (expand21(qx) << 2) | (expand21(qy) << 1) | expand21(qz);
+    if (MODE == NBODY_KEYS_MORTON) {
+        const uint64_t qx = quantize21(p.x, box[0], box[3]);
+        const uint64_t qy = quantize21(p.y, box[1], box[4]);
+        const uint64_t qz = quantize21(p.z, box[2], box[5]);
+        keys[i] = (expand21(qx) << 2) | (expand21(qy) << 1) | expand21(qz);
+    } else {
+        keys[i] = octree_key(p.x, p.y, p.z, box);
+    }
     if (vals) vals[i] = static_cast<uint32_t>(i);
 }
 
@@ -248,84 +301,163 @@ __device__ __forceinline__ float cell_side2(uint64_t key, int L, const float *__
     return __fmul_rn(s, s);
 }
 
+// Record index of the cell whose top radix-tree node is p.
+__device__ __forceinline__ int record_of(const BinaryTree &t, const uint32_t *__restrict__ mask,
+                                         const uint32_t *__restrict__ P, int p) {
+    const int L = level_of(t.delta[p]);
+    const int lo = t.lo[p];
+    return static_cast<int>(P[lo] + __popc(mask[lo] & ((1u << L) - 1u)));
+}
+
+// Octree parent of a record: the nearest radix-tree ancestor that is a cell
+// top (the nodes in between split the same cell; at most 6 of them).
+__device__ __forceinline__ int octree_parent(const BinaryTree &t, const uint32_t *__restrict__ mask,
+                                             const uint32_t *__restrict__ P, int p) {
+    for (int guard = 0; p >= 0 && !t.top[p] && guard < 96; ++guard) p = t.iparent[p];
+    return (p >= 0 && t.top[p]) ? record_of(t, mask, P, p) : -1;
+}
+
 __global__ void emit_cells_kernel(const uint64_t *__restrict__ k, int64_t n, BinaryTree t,
                                   const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
-                                  const float *__restrict__ box, BHNode *__restrict__ nodes) {
+                                  const float *__restrict__ box, BHNode *__restrict__ nodes, Records r) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
-    if (!t.top[i]) {
-        t.top_index[i] = -1;
-        return;
-    }
+    if (!t.top[i]) return;
     const int L = level_of(t.delta[i]);
     const int lo = t.lo[i], hi = t.hi[i];
-    const uint32_t idx = P[lo] + __popc(mask[lo] & ((1u << L) - 1u));
-    t.top_index[i] = static_cast<int>(idx);
+    const int idx = record_of(t, mask, P, static_cast<int>(i));
     int4 meta;
     if (L < kMaxLevel) {
         meta = make_int4(__float_as_int(cell_side2(k[lo], L, box)), static_cast<int>(P[hi + 1]), lo, 0);
-    } else {  // bucket of bodies with identical keys
+    } else {  // bucket of bodies with identical keys: a leaf
         meta = make_int4(__float_as_int(-1.f), static_cast<int>(P[hi + 1]), lo, hi - lo + 1);
     }
     nodes[idx].meta = meta;
+    r.level[idx] = L;
+    const int par = i == 0 ? -1 : octree_parent(t, mask, P, t.iparent[i]);
+    r.parent[idx] = par;
+    if (par >= 0) atomicAdd(&r.nchild[par], 1);
 }
 
 __global__ void emit_leaves_kernel(const uint64_t *__restrict__ k, int64_t n, const float4 *__restrict__ pos,
-                                   const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
-                                   BHNode *__restrict__ nodes) {
+                                   BinaryTree t, const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
+                                   BHNode *__restrict__ nodes, Records r) {
     const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (b >= n) return;
     const bool lone = !((b > 0 && k[b] == k[b - 1]) || (b + 1 < n && k[b] == k[b + 1]));
     if (!lone) return;
-    const uint32_t idx = P[b] + __popc(mask[b]);
+    const int idx = static_cast<int>(P[b] + __popc(mask[b]));
     nodes[idx].cm = pos[b];
     nodes[idx].meta = make_int4(__float_as_int(-1.f), static_cast<int>(P[b + 1]), static_cast<int>(b), 1);
+    r.level[idx] = kMaxLevel + 1;  // a lone body
+    const int par = n < 2 ? -1 : octree_parent(t, mask, P, t.lparent[b]);
+    r.parent[idx] = par;
+    if (par >= 0) atomicAdd(&r.nchild[par], 1);
 }
 
-// Bottom-up mass and mass-weighted position sums over the radix tree; the
-// second child to arrive at a node combines both (left + right, fixed order).
-// Prefix lengths strictly grow from parent to child (at most 63 key bits plus
-// 32 tie-break bits), so no body climbs more than 96 nodes.
-constexpr int kMaxRadixDepth = 128;
+// The reference's child order (Octree::getNextNode, src/Octree/Octree.cpp:148-153):
+// index bit a is set when the body lies below the centre on axis a (x = bit 0),
+// while a Morton digit bit is set for the upper half (x = bit 2).
+__device__ __forceinline__ int reference_child_index(uint32_t digit) {
+    return static_cast<int>(((~digit >> 2) & 1u) | ((~digit) & 2u) | (((~digit) & 1u) << 2));
+}
 
-__global__ void upsweep_kernel(int64_t n, const float4 *__restrict__ pos, BinaryTree t,
-                               unsigned *__restrict__ arrivals, float4 *__restrict__ msum,
-                               BHNode *__restrict__ nodes, int *status) {
-    const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (b >= n || n < 2) return;
-    int p = t.lparent[b];
-    for (int depth = 0; p >= 0; ++depth) {
-        if (depth >= kMaxRadixDepth) {
-            record_error(status, NBODY_ERR_CAPACITY);
-            return;
-        }
-        __threadfence();
-        if (atomicAdd(&arrivals[p], 1u) == 0u) return;
-        __threadfence();
-        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-        const int ch[2] = {t.left[p], t.right[p]};
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            float4 v;
-            if (ch[c] < 0) {
-                const float4 q = pos[~ch[c]];
-                v = make_float4(q.x * q.w, q.y * q.w, q.z * q.w, q.w);
-            } else {
-                v = __ldcg(&msum[ch[c]]);
-            }
-            acc.x += v.x;
-            acc.y += v.y;
-            acc.z += v.z;
-            acc.w += v.w;
-        }
-        msum[p] = acc;
-        const int idx = t.top_index[p];
-        if (idx >= 0) {
-            const float m = acc.w;
-            nodes[idx].cm = m > 0.f ? make_float4(acc.x / m, acc.y / m, acc.z / m, m) : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        p = t.iparent[p];
+// Bottom-up centres of mass in the reference's arithmetic
+// (ParallelOctreeCPU::propagate / Octree::propagate, Octree.cpp:238-258): a
+// cell's centre is sum(child centre * child mass) / sum(child mass) over its
+// occupied children in the reference's child order, every step rounded on its
+// own. A cell of the reference's tree that has a single occupied child is
+// skipped here but leaves its trace: (c * m) / m once per skipped level. The
+// reference also keeps lone bodies no shallower than its fixed top levels
+// (depth `father_depth`). The last child to finish computes its parent; a
+// cell all of whose children are leaves is flagged (meta.w = -bodies) so the
+// traversal can sum its bodies directly.
+__device__ __forceinline__ float4 round_trips(float4 c, int times) {
+    for (int q = 0; q < times; ++q) {
+        c.x = __fdiv_rn(__fmul_rn(c.x, c.w), c.w);
+        c.y = __fdiv_rn(__fmul_rn(c.y, c.w), c.w);
+        c.z = __fdiv_rn(__fmul_rn(c.z, c.w), c.w);
     }
+    return c;
+}
+
+__global__ void upsweep_kernel(const uint64_t *__restrict__ k, int64_t n, const float4 *__restrict__ pos,
+                               const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
+                               BHNode *__restrict__ nodes, Records r, int father_depth, int *status) {
+    const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    const bool left_eq = b > 0 && k[b] == k[b - 1];
+    const bool right_eq = b + 1 < n && k[b] == k[b + 1];
+    int rec;
+    if (!left_eq && !right_eq) {
+        rec = static_cast<int>(P[b] + __popc(mask[b]));  // lone body: already written
+    } else if (!left_eq) {
+        // first body of a bucket: its record is the level-21 cell starting here
+        rec = static_cast<int>(P[b] + __popc(mask[b] & ((1u << kMaxLevel) - 1u)));
+        float cx = 0.f, cy = 0.f, cz = 0.f, m = 0.f;
+        for (int64_t q = b; q < n && k[q] == k[b]; ++q) {
+            const float4 o = pos[q];
+            if (!(o.w > 0.f)) continue;
+            cx = __fadd_rn(cx, __fmul_rn(o.x, o.w));
+            cy = __fadd_rn(cy, __fmul_rn(o.y, o.w));
+            cz = __fadd_rn(cz, __fmul_rn(o.z, o.w));
+            m = __fadd_rn(m, o.w);
+        }
+        nodes[rec].cm = m > 0.f ? make_float4(__fdiv_rn(cx, m), __fdiv_rn(cy, m), __fdiv_rn(cz, m), m)
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+        return;
+    }
+    for (int depth = 0; depth <= kMaxLevel + 2; ++depth) {
+        const int par = r.parent[rec];
+        if (par < 0) return;
+        __threadfence();
+        const int done = static_cast<int>(atomicAdd(&r.arrive[par], 1u)) + 1;
+        if (done < __ldcg(&r.nchild[par])) return;
+        __threadfence();
+        const int L = __ldcg(&r.level[par]);
+        const int4 pm = __ldcg(&nodes[par].meta);
+        float4 slot[8];
+        bool used[8] = {false, false, false, false, false, false, false, false};
+        bool all_leaves = true;
+        int bodies = 0;
+        int c = par + 1;
+        for (int guard = 0; c < pm.y && guard < 8; ++guard) {
+            const int4 cmeta = __ldcg(&nodes[c].meta);
+            float4 cc = __ldcg(&nodes[c].cm);
+            const int cl = __ldcg(&r.level[c]);
+            const uint32_t digit = static_cast<uint32_t>(k[cmeta.z] >> (63 - 3 * (L + 1))) & 7u;
+            int trips;
+            if (cl > kMaxLevel || cl == kMaxLevel) {  // a leaf (lone body or bucket)
+                trips = father_depth - (L + 1) > 0 ? father_depth - (L + 1) : 0;
+                bodies += cmeta.w;
+            } else {
+                trips = cl - L - 1;
+                all_leaves = false;
+            }
+            if (cc.w > 0.f) {
+                const int j = reference_child_index(digit);
+                slot[j] = round_trips(cc, trips);
+                used[j] = true;
+            }
+            c = cmeta.y;
+        }
+        if (c != pm.y) record_error(status, NBODY_ERR_CAPACITY);  // more than 8 children: broken tree
+        float cx = 0.f, cy = 0.f, cz = 0.f, m = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (!used[j]) continue;
+            cx = __fadd_rn(cx, __fmul_rn(slot[j].x, slot[j].w));
+            cy = __fadd_rn(cy, __fmul_rn(slot[j].y, slot[j].w));
+            cz = __fadd_rn(cz, __fmul_rn(slot[j].z, slot[j].w));
+            m = __fadd_rn(m, slot[j].w);
+        }
+        nodes[par].cm = m > 0.f ? make_float4(__fdiv_rn(cx, m), __fdiv_rn(cy, m), __fdiv_rn(cz, m), m)
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (all_leaves) nodes[par].meta.w = -bodies;
+        rec = par;
+    }
+    record_error(status, NBODY_ERR_CAPACITY);  // deeper than any octree: broken tree
 }
 
 // --------------------------------------------------------------- traversal
@@ -356,40 +488,51 @@ __global__ void __launch_bounds__(256) traverse_kernel(const BHNode *__restrict_
     while (i < m_nodes) {
         const float4 cm = __ldg(&nodes[i].cm);
         const int4 meta = __ldg(&nodes[i].meta);
-        bool open = false;
-        if (skip <= i) {
-            const float dx = __fsub_rn(cm.x, me.x), dy = __fsub_rn(cm.y, me.y), dz = __fsub_rn(cm.z, me.z);
-            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-            const float s2 = __int_as_float(meta.x);
-            if (s2 < 0.f || s2 < __fmul_rn(theta2, d2)) {
-                if (meta.w >= 2) {
-                    const int q1 = meta.z + meta.w < n ? meta.z + meta.w : static_cast<int>(n);
-                    for (int q = meta.z < 0 ? 0 : meta.z; q < q1; ++q) {
-                        const float4 o = pos[q];
-                        const float ex = o.x - me.x, ey = o.y - me.y, ez = o.z - me.z;
-                        const float e2 = __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
-                        if (o.w > 0.f && e2 > 0.f) {
-                            if (COUNT) ++n_pairs;
-                            const float inv = rsqrt_ftz(e2 + eps2);
-                            const float w = o.w * inv * inv * inv;
-                            fx = fmaf(ex, w, fx);
-                            fy = fmaf(ey, w, fy);
-                            fz = fmaf(ez, w, fz);
-                        }
+        const bool act = skip <= i;
+        const float dx = __fsub_rn(cm.x, me.x), dy = __fsub_rn(cm.y, me.y), dz = __fsub_rn(cm.z, me.z);
+        const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+        const float s2 = __int_as_float(meta.x);
+        // Octree.cpp:318: accept a leaf, or a cell with s^2 < theta^2 d^2.
+        const bool acc = act && (s2 < 0.f || s2 < __fmul_rn(theta2, d2));
+        // Force from the record itself (a cell's centre of mass or a lone
+        // body). A branch, not a select: records every active lane opens (the
+        // upper levels) then cost no force arithmetic at all.
+        if (acc && meta.w <= 1 && cm.w > 0.f && d2 > 0.f) {
+            if (COUNT) ++n_pairs;
+            const float inv = rsqrt_ftz(d2 + eps2);
+            const float w = cm.w * inv * inv * inv;
+            fx = fmaf(dx, w, fx);
+            fy = fmaf(dy, w, fy);
+            fz = fmaf(dz, w, fz);
+        }
+        if (meta.w != 0 && meta.w != 1) {  // warp-uniform: a bucket or a terminal cell
+            // A bucket (meta.w >= 2) accepted, or a terminal cell (meta.w < 0)
+            // opened: every body in it interacts one by one.
+            if ((meta.w >= 2 && acc) || (meta.w < 0 && act && !acc)) {
+                const int cntb = meta.w >= 2 ? meta.w : -meta.w;
+                const int q0 = meta.z < 0 ? 0 : meta.z;
+                const int q1 = meta.z + cntb < n ? meta.z + cntb : static_cast<int>(n);
+                for (int q = q0; q < q1; ++q) {
+                    const float4 o = pos[q];
+                    const float ex = __fsub_rn(o.x, me.x), ey = __fsub_rn(o.y, me.y), ez = __fsub_rn(o.z, me.z);
+                    const float e2 =
+                        __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
+                    if (o.w > 0.f && e2 > 0.f) {
+                        if (COUNT) ++n_pairs;
+                        const float iv = rsqrt_ftz(e2 + eps2);
+                        const float wq = o.w * iv * iv * iv;
+                        fx = fmaf(ex, wq, fx);
+                        fy = fmaf(ey, wq, fy);
+                        fz = fmaf(ez, wq, fz);
                     }
-                } else if (cm.w > 0.f && d2 > 0.f) {
-                    if (COUNT) ++n_pairs;
-                    const float inv = rsqrt_ftz(d2 + eps2);
-                    const float w = cm.w * inv * inv * inv;
-                    fx = fmaf(dx, w, fx);
-                    fy = fmaf(dy, w, fy);
-                    fz = fmaf(dz, w, fz);
                 }
-                skip = meta.y;
-            } else {
-                open = true;
             }
         }
+        // A lane is done with this subtree if it accepted the record or summed
+        // a terminal cell's bodies; otherwise an active lane opens it.
+        const bool done = acc || (act && meta.w < 0);
+        if (done) skip = meta.y;
+        const bool open = act && !done;
         if (COUNT) ++n_visits;
         if (__any_sync(0xffffffffu, open)) {
             ++i;
@@ -540,6 +683,21 @@ __global__ void scan_add_kernel(uint32_t *__restrict__ out, int64_t n, const uin
 
 unsigned grid_for(int64_t n, int threads) { return static_cast<unsigned>((n + threads - 1) / threads); }
 
+// Depth of the reference's fully expanded top levels for n bodies
+// (ParallelOctreeCPU::ParallelOctreeCPU, src/Octree/ParallelOctreeCPU.cpp:7-23):
+// the deepest d <= 3 with 1 + 8 + ... + 8^d < n.
+int father_depth(int64_t n) {
+    int64_t nodes = 0, p8 = 1;
+    int d = -1;
+    while (nodes < n && d < 3) {
+        if (nodes + p8 >= n) break;
+        nodes += p8;
+        ++d;
+        p8 *= 8;
+    }
+    return d;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------- host
@@ -575,9 +733,10 @@ size_t bh_workspace_layout(int64_t n, void *base, BHWorkspace *w) {
     w->tree.iparent = static_cast<int *>(take(sizeof(int) * nn));
     w->tree.lparent = static_cast<int *>(take(sizeof(int) * nn));
     w->tree.top = static_cast<int *>(take(sizeof(int) * nn));
-    w->tree.top_index = static_cast<int *>(take(sizeof(int) * nn));
-    w->arrivals = static_cast<unsigned *>(take(sizeof(unsigned) * nn));
-    w->msum = static_cast<float4 *>(take(sizeof(float4) * nn));
+    w->rec.level = static_cast<int *>(take(sizeof(int) * 2 * nn));
+    w->rec.parent = static_cast<int *>(take(sizeof(int) * 2 * nn));
+    w->rec.nchild = static_cast<int *>(take(sizeof(int) * 2 * nn));
+    w->rec.arrive = static_cast<unsigned *>(take(sizeof(unsigned) * 2 * nn));
     w->mask = static_cast<uint32_t *>(take(sizeof(uint32_t) * nn));
     w->cnt = static_cast<uint32_t *>(take(sizeof(uint32_t) * nn));
     w->P = static_cast<uint32_t *>(take(sizeof(uint32_t) * (nn + 1)));
@@ -599,9 +758,12 @@ cudaError_t bh_bbox(const float4 *pos, int64_t n, BHWorkspace &w, cudaStream_t s
     return cudaGetLastError();
 }
 
-cudaError_t bh_keys(const float4 *pos, int64_t n, BHWorkspace &w, cudaStream_t st, StageTimer *timer) {
+cudaError_t bh_keys(const float4 *pos, int64_t n, BHWorkspace &w, int mode, cudaStream_t st, StageTimer *timer) {
     if (timer) timer->begin(kStageMorton, st);
-    morton_kernel<<<grid_for(n, 256), 256, 0, st>>>(pos, n, w.box, w.keys[0], w.vals[0]);
+    if (mode == NBODY_KEYS_MORTON)
+        morton_kernel<NBODY_KEYS_MORTON><<<grid_for(n, 256), 256, 0, st>>>(pos, n, w.box, w.keys[0], w.vals[0]);
+    else
+        morton_kernel<NBODY_KEYS_OCTREE><<<grid_for(n, 256), 256, 0, st>>>(pos, n, w.box, w.keys[0], w.vals[0]);
     if (timer) timer->end(kStageMorton, st);
     return cudaGetLastError();
 }
@@ -644,17 +806,17 @@ cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaSt
     scan_tiles_kernel<<<tiles, kScanThreads, 0, st>>>(w.cnt, n, w.P, w.scan_sums);
     scan_sums_kernel<<<1, 1024, 0, st>>>(w.scan_sums, tiles, w.P + n);
     scan_add_kernel<<<grid_for(n, 256), 256, 0, st>>>(w.P, n, w.scan_sums);
+    const size_t nrec = 2 * static_cast<size_t>(n > 1 ? n : 2);
+    e = cudaMemsetAsync(w.rec.nchild, 0, sizeof(int) * nrec, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.rec.arrive, 0, sizeof(unsigned) * nrec, st);
+    if (e != cudaSuccess) return e;
     if (n >= 2)
-        emit_cells_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(k, n, w.tree, w.mask, w.P, w.box, w.nodes);
-    emit_leaves_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.mask, w.P, w.nodes);
+        emit_cells_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(k, n, w.tree, w.mask, w.P, w.box, w.nodes, w.rec);
+    emit_leaves_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.tree, w.mask, w.P, w.nodes, w.rec);
     if (timer) timer->end(kStageBuild, st);
     if (timer) timer->begin(kStageUpsweep, st);
-    if (n >= 2) {
-        e = cudaMemsetAsync(w.arrivals, 0, sizeof(unsigned) * static_cast<size_t>(n - 1), st);
-        if (e != cudaSuccess) return e;
-        upsweep_kernel<<<grid_for(n, 256), 256, 0, st>>>(n, pos_sorted, w.tree, w.arrivals, w.msum, w.nodes,
-                                                         status);
-    }
+    upsweep_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.mask, w.P, w.nodes, w.rec,
+                                                     father_depth(n), status);
     if (timer) timer->end(kStageUpsweep, st);
     return cudaGetLastError();
 }

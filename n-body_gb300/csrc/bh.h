@@ -14,7 +14,8 @@ constexpr int kBBoxBlocks = 1024;
 // One pre-order tree record (32 bytes). cm = centre of mass and mass (for a
 // lone-body leaf: its position and mass). meta.x = s^2 of the cell as float
 // bits (-1 for leaves), meta.y = next record after the subtree, meta.z =
-// first body (sorted order), meta.w = body count of a leaf (0 for cells).
+// first body (sorted order), meta.w = body count of a leaf, 0 for a cell, or
+// minus the body count of a cell whose children are all leaves.
 struct __align__(16) BHNode {
     float4 cm;
     int4 meta;
@@ -23,7 +24,14 @@ struct __align__(16) BHNode {
 // Binary radix tree over sorted keys: internal node i covers bodies
 // [lo, hi]; a child < 0 is body ~child.
 struct BinaryTree {
-    int *lo, *hi, *left, *right, *delta, *iparent, *lparent, *top, *top_index;
+    int *lo, *hi, *left, *right, *delta, *iparent, *lparent, *top;
+};
+
+// Per-record bookkeeping for the bottom-up pass: cell level (kMaxLevel + 1
+// for a lone body), octree parent record, child count, arrivals.
+struct Records {
+    int *level, *parent, *nchild;
+    unsigned *arrive;
 };
 
 struct BHWorkspace {
@@ -35,8 +43,7 @@ struct BHWorkspace {
     float *bbox_partial = nullptr;
     unsigned *bbox_counter = nullptr;
     BinaryTree tree{};
-    unsigned *arrivals = nullptr;
-    float4 *msum = nullptr;
+    Records rec{};
     uint32_t *mask = nullptr;
     uint32_t *cnt = nullptr;
     uint32_t *P = nullptr;  // n + 1 entries; P[n] = record count
@@ -56,7 +63,8 @@ size_t bh_workspace_bytes(int64_t n);
 size_t bh_workspace_layout(int64_t n, void *base, BHWorkspace *w);
 
 cudaError_t bh_bbox(const float4 *pos, int64_t n, BHWorkspace &w, cudaStream_t st, StageTimer *timer);
-cudaError_t bh_keys(const float4 *pos, int64_t n, BHWorkspace &w, cudaStream_t st, StageTimer *timer);
+// Keys of `mode` (NBODY_KEYS_OCTREE or NBODY_KEYS_MORTON) into keys[0], index into vals[0].
+cudaError_t bh_keys(const float4 *pos, int64_t n, BHWorkspace &w, int mode, cudaStream_t st, StageTimer *timer);
 cudaError_t bh_sort(int64_t n, BHWorkspace &w, cudaStream_t st, int *status, StageTimer *timer);
 cudaError_t bh_gather(int64_t n, const BHWorkspace &w, const float4 *pos_in, const float4 *vel_in,
                       const float4 *acc_in, const int *id_in, float4 *pos_out, float4 *vel_out, float4 *acc_out,

@@ -100,6 +100,7 @@ struct nbody_ctx {
     float4 *acc2[2] = {nullptr, nullptr};
     int *ids[2] = {nullptr, nullptr};
     int bh_pos = 0, bh_va = 0;
+    int key_mode = NBODY_KEYS_OCTREE;
     bool ids_valid = false;  // false until the first step after an upload
     // Barnes-Hut workspace (keys, sort scratch, tree), grown on demand.
     void *ws_mem = nullptr;
@@ -211,7 +212,7 @@ int bh_step(nbody_ctx *ctx) {
     int *Io = ctx->ids[ctx->bh_va ^ 1];
     nbody::StageTimer *tm = ctx->timer;
     NB_CK(ctx, nbody::bh_bbox(P, n, w, ctx->stream, tm));
-    NB_CK(ctx, nbody::bh_keys(P, n, w, ctx->stream, tm));
+    NB_CK(ctx, nbody::bh_keys(P, n, w, ctx->key_mode, ctx->stream, tm));
     NB_CK(ctx, nbody::bh_sort(n, w, ctx->stream, ctx->status, tm));
     NB_CK(ctx, nbody::bh_gather(n, w, P, V, A, I, Po, Vo, Ao, Io, ctx->stream, ctx->status, tm));
     NB_CK(ctx, nbody::bh_build(Po, n, w, ctx->stream, ctx->status, tm));
@@ -445,7 +446,7 @@ int nbody_bh_keys_device(nbody_ctx *ctx, const void *pos_mass4, int64_t n, void 
     nbody::BHWorkspace &w = ctx->ws;
     const float4 *p = static_cast<const float4 *>(pos_mass4);
     NB_CK(ctx, nbody::bh_bbox(p, n, w, ctx->stream, ctx->timer));
-    NB_CK(ctx, nbody::bh_keys(p, n, w, ctx->stream, ctx->timer));
+    NB_CK(ctx, nbody::bh_keys(p, n, w, ctx->key_mode, ctx->stream, ctx->timer));
     if (keys_out)
         NB_CK(ctx, cudaMemcpyAsync(keys_out, w.keys[0], sizeof(uint64_t) * static_cast<size_t>(n),
                                    cudaMemcpyDeviceToDevice, ctx->stream));
@@ -493,7 +494,7 @@ int nbody_bh_forces_device(nbody_ctx *ctx, const void *pos_mass4, void *force4, 
     const float4 *p = static_cast<const float4 *>(pos_mass4);
     nbody::StageTimer *tm = ctx->timer;
     NB_CK(ctx, nbody::bh_bbox(p, n, w, ctx->stream, tm));
-    NB_CK(ctx, nbody::bh_keys(p, n, w, ctx->stream, tm));
+    NB_CK(ctx, nbody::bh_keys(p, n, w, ctx->key_mode, ctx->stream, tm));
     NB_CK(ctx, nbody::bh_sort(n, w, ctx->stream, ctx->status, tm));
     NB_CK(ctx, nbody::bh_gather(n, w, p, nullptr, nullptr, nullptr, ctx->dev_pos, nullptr, nullptr, ctx->dev_ids,
                                 ctx->stream, ctx->status, tm));
@@ -607,6 +608,12 @@ int nbody_profile_read(nbody_ctx *ctx, double *ms, int *launches, int nstages) {
     if (!ctx->timer) return NBODY_OK;
     DeviceGuard dg(ctx->device);
     NB_CK(ctx, ctx->timer->read(ms, launches, nstages));
+    return NBODY_OK;
+}
+
+int nbody_set_key_mode(nbody_ctx *ctx, int mode) {
+    if (!ctx || (mode != NBODY_KEYS_OCTREE && mode != NBODY_KEYS_MORTON)) return NBODY_ERR_ARG;
+    ctx->key_mode = mode;
     return NBODY_OK;
 }
 

@@ -27,6 +27,7 @@ LIB_PATH = os.path.join(HERE, "libnbody_gb300.so")
 
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_CAPACITY, ERR_TIMEOUT, ERR_STATE = range(7)
 MODE_PP, MODE_BH = 0, 1
+KEYS_OCTREE, KEYS_MORTON = 0, 1
 _MODES = {"pp": MODE_PP, "bh": MODE_BH, MODE_PP: MODE_PP, MODE_BH: MODE_BH}
 
 _lib = None
@@ -64,6 +65,7 @@ SIGNATURES = {
     "nbody_bh_forces_device": (_i, [_vp, _vp, _vp, _i64]),
     "nbody_bh_tree_export": (_i, [_vp, _vp, _i64, ctypes.POINTER(_i64), _vp]),
     "nbody_bh_counters": (_i, [_vp, _i, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "nbody_set_key_mode": (_i, [_vp, _i]),
 }
 
 
@@ -276,6 +278,11 @@ class ParticleSolverCUDA:
                     "nbody_bh_tree_export")
         rec = rec[:m]
         return rec[:, :4].copy(), rec[:, 4:].view(np.int32).copy(), box
+
+    def set_key_mode(self, mode) -> None:
+        """'octree' (the reference's FP32 cell descent, default) or 'morton' (morton.glsl quantisation)."""
+        m = {"octree": KEYS_OCTREE, "morton": KEYS_MORTON}.get(mode, mode)
+        self._check(lib().nbody_set_key_mode(self._ctx, int(m)), "nbody_set_key_mode")
 
     def bh_counters(self, enable: bool):
         """(pair evaluations, warp record visits) since the last call; then counting on/off."""

@@ -52,6 +52,36 @@ void orc_morton63(int64_t n, const float *pos4, const float bmin[3], const float
     for (int64_t i = 0; i < n; ++i) keys[i] = orc_morton63_key(pos4[4 * i], pos4[4 * i + 1], pos4[4 * i + 2], bmin, bmax);
 }
 
+/* ---- octree-descent keys ------------------------------------------------
+ * The reference's own child selection, Octree::getNextNode with the child
+ * boxes of Octree::subdivide (src/Octree/Octree.cpp:148-231), applied 21 times
+ * from the root box: per level and axis, centre = min + (max - min) / 2 and the
+ * body goes to the upper half unless pos < centre; key bit 1 = upper half, x
+ * highest in each triple. */
+uint64_t orc_octree_key(float px, float py, float pz, const float bmin[3], const float bmax[3]) {
+    float mn[3] = {bmin[0], bmin[1], bmin[2]};
+    float mx[3] = {bmax[0], bmax[1], bmax[2]};
+    const float p[3] = {px, py, pz};
+    uint64_t key = 0;
+    for (int l = 0; l < 21; ++l) {
+        uint64_t digit = 0;
+        for (int a = 0; a < 3; ++a) {
+            const float w = mx[a] - mn[a];
+            const float c = mn[a] + w / 2.f;
+            const int upper = !(p[a] < c);
+            if (upper) mn[a] = c; else mx[a] = c;
+            digit |= (uint64_t)upper << (2 - a);
+        }
+        key = (key << 3) | digit;
+    }
+    return key;
+}
+
+void orc_octree_keys(int64_t n, const float *pos4, const float bmin[3], const float bmax[3], uint64_t *keys) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) keys[i] = orc_octree_key(pos4[4 * i], pos4[4 * i + 1], pos4[4 * i + 2], bmin, bmax);
+}
+
 /* ---- stable sort: LSD radix, 8 bits per pass (stable by construction) ---- */
 int orc_sort_stable(int64_t n, const uint64_t *keys, uint64_t *keys_sorted, uint32_t *perm) {
     if (n < 0) return ORC_ERR_ARG;

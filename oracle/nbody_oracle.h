@@ -36,6 +36,10 @@ void orc_bbox(int64_t n, const float *pos4, float bmin[3], float bmax[3]);
 uint64_t orc_morton63_key(float px, float py, float pz, const float bmin[3], const float bmax[3]);
 void orc_morton63(int64_t n, const float *pos4, const float bmin[3], const float bmax[3], uint64_t *keys);
 
+/* Keys from the reference's octree descent (Octree::getNextNode), 21 levels. */
+uint64_t orc_octree_key(float px, float py, float pz, const float bmin[3], const float bmax[3]);
+void orc_octree_keys(int64_t n, const float *pos4, const float bmin[3], const float bmax[3], uint64_t *keys);
+
 /* Stable LSD radix argsort of 64-bit keys: perm[r] = index of the r-th smallest
  * key, ties kept in index order. keys_sorted may be NULL. */
 int orc_sort_stable(int64_t n, const uint64_t *keys, uint64_t *keys_sorted, uint32_t *perm);

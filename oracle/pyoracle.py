@@ -53,6 +53,7 @@ def port():
         lib = ctypes.CDLL(PORT_SO)
         lib.orc_bbox.argtypes = [ctypes.c_int64, _f, _f, _f]
         lib.orc_morton63.argtypes = [ctypes.c_int64, _f, _f, _f, _u64]
+        lib.orc_octree_keys.argtypes = [ctypes.c_int64, _f, _f, _f, _u64]
         lib.orc_sort_stable.argtypes = [ctypes.c_int64, _u64, _u64, _u32]
         lib.orc_pp_forces.argtypes = [ctypes.c_int64, _f, _f, ctypes.c_float, _f, ctypes.c_int]
         lib.orc_integrate.argtypes = [ctypes.c_int64, _f, _f, _f, _f, ctypes.c_float, ctypes.c_int]
@@ -104,6 +105,14 @@ def morton63(pos4, bmin, bmax):
     keys = np.zeros(len(pos4), np.uint64)
     port().orc_morton63(len(pos4), _p(pos4), _p(np.asarray(bmin, np.float32)), _p(np.asarray(bmax, np.float32)),
                         _p(keys, _u64))
+    return keys
+
+
+def octree_keys(pos4, bmin, bmax):
+    pos4 = _f4(pos4)
+    keys = np.zeros(len(pos4), np.uint64)
+    port().orc_octree_keys(len(pos4), _p(pos4), _p(np.asarray(bmin, np.float32)), _p(np.asarray(bmax, np.float32)),
+                           _p(keys, _u64))
     return keys
 
 

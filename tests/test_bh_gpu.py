@@ -51,8 +51,9 @@ def bh_forces(nb, torch, pos, mass, eps2=40.0, theta2=0.25):
 
 
 # ------------------------------------------------------------------ keys / box
+@pytest.mark.parametrize("mode", ["octree", "morton"])
 @pytest.mark.parametrize("kind", ["ball", "plummer", "negative_axis", "flat"])
-def test_box_and_morton_keys_bit_exact(nb, cuda, oracle, kind):
+def test_box_and_keys_bit_exact(nb, cuda, oracle, kind, mode):
     torch = cuda
     from nbody_gb300 import initializers as I
 
@@ -68,6 +69,7 @@ def test_box_and_morton_keys_bit_exact(nb, cuda, oracle, kind):
         pos, _, mass = I.uniform_ball(n, seed=24)
         pos[:, 2] = 3.0
     s = solver_for(nb, n)
+    s.set_key_mode(mode)
     pm = torch.from_numpy(I.pos_mass(pos, mass)).cuda()
     keys = torch.zeros(n, dtype=torch.int64, device="cuda")
     box = torch.zeros(6, dtype=torch.float32, device="cuda")
@@ -75,7 +77,7 @@ def test_box_and_morton_keys_bit_exact(nb, cuda, oracle, kind):
     s.sync()
     mn, mx = oracle.bbox(pos)
     np.testing.assert_array_equal(box.cpu().numpy(), np.concatenate([mn, mx]))
-    ref = oracle.morton63(pos, mn, mx)
+    ref = oracle.octree_keys(pos, mn, mx) if mode == "octree" else oracle.morton63(pos, mn, mx)
     np.testing.assert_array_equal(keys.cpu().numpy().view(np.uint64), ref)
 
 
@@ -169,6 +171,14 @@ def test_tree_invariants(nb, cuda, oracle, kind):
         covered[f:f + c] += 1
     assert np.all(covered == 1)
     assert np.all(np.diff(first[leaf]) > 0)
+    # a cell flagged terminal (meta.w < 0) has only leaves below it, -meta.w of them
+    term = cell & (cnt < 0)
+    assert term.sum() > 0
+    for i in np.flatnonzero(term)[:2000]:
+        sub = np.arange(i + 1, nxt[i])
+        assert np.all(leaf[sub]), i
+        assert -cnt[i] == cnt[sub].sum()
+    assert np.all(cnt[cell & ~term] == 0)
     # cell masses equal the sum of the leaves in their subtree
     leaf_mass = np.where(leaf, cm[:, 3].astype(np.float64), 0.0)
     csum = np.concatenate([[0.0], np.cumsum(leaf_mass)])
@@ -177,7 +187,7 @@ def test_tree_invariants(nb, cuda, oracle, kind):
     # cell sides: the reference's FP32 halving of the root box
     mn, mx = oracle.bbox(pos)
     np.testing.assert_array_equal(box, np.concatenate([mn, mx]))
-    keys = np.sort(oracle.morton63(pos, mn, mx))
+    keys = np.sort(oracle.octree_keys(pos, mn, mx))
     rng = np.random.default_rng(0)
     for i in rng.choice(np.flatnonzero(cell), size=min(300, int(cell.sum())), replace=False):
         body = first[i]

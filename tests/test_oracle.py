@@ -142,6 +142,34 @@ def test_morton_corners_and_monotone(oracle):
     assert np.all(kx2 >= kx)
 
 
+def test_octree_keys_follow_reference_descent(oracle):
+    """Octree-descent keys vs a direct Python restatement of
+    Octree::getNextNode / Octree::subdivide in float32, and they agree with the
+    morton.glsl quantisation except within rounding of cell boundaries."""
+    rng = np.random.default_rng(3)
+    p = rng.uniform(-50, 70, size=(3000, 4)).astype(np.float32)
+    p[:, 3] = 0
+    mn, mx = oracle.bbox(p)
+    keys = oracle.octree_keys(p, mn, mx)
+    f = np.float32
+    for i in range(0, 3000, 97):
+        lo, hi, key = mn.copy(), mx.copy(), 0
+        for _ in range(21):
+            d = 0
+            for a in range(3):
+                c = f(lo[a] + f(f(hi[a] - lo[a]) / f(2)))
+                up = not (p[i, a] < c)
+                if up:
+                    lo[a] = c
+                else:
+                    hi[a] = c
+                d |= int(up) << (2 - a)
+            key = (key << 3) | d
+        assert int(keys[i]) == key
+    mk = oracle.morton63(p, mn, mx)
+    assert np.mean(keys >> np.uint64(33) == mk >> np.uint64(33)) > 0.99
+
+
 def test_bbox_reference_seed_quirk(oracle):
     # max seeds are FLT_MIN (ParallelOctreeCPU.cpp:80): an all-negative axis keeps max = FLT_MIN
     pos = np.array([[-1, 1, -5, 0], [-2, 3, -4, 0]], np.float32)
