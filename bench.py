@@ -365,7 +365,7 @@ def bench_bh(args, world, rank, local, dist):
                 "kernel": "traverse_kernel", "kernel_ms_per_launch": round(t_launch * 1e3, 4),
                 "work": {"pair_evaluations_per_step": pairs, "per_body": round(pairs / n, 1),
                          "warp_record_visits_per_step": visits,
-                         "lane_efficiency": round(pairs / max(1, visits * 32), 4)},
+                         "pair_evaluations_per_warp_visit": round(pairs / max(1, visits), 2)},
                 "peak_note": f"nominal FP32 FMA peak ({sms} SMs x 128 lanes x 2 flop x {pk.get('sm_max_mhz')} MHz, "
                              f"{pk['source']} peaks file); 20 flop per pairwise evaluation, as for the direct sum. "
                              f"The traversal is latency/issue-bound; the other stages are graded against "

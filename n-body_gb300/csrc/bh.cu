@@ -578,6 +578,139 @@ __global__ void __launch_bounds__(256) traverse_kernel(const BHNode *__restrict_
     }
 }
 
+// Two bodies per lane: a warp serves 64 consecutive sorted bodies (lane l
+// holds bodies base + l and base + 32 + l), so each record load, vote and
+// branch is shared by twice the bodies. The criterion and forces use packed
+// f32x2 arithmetic, each lane of a pair rounded exactly as the scalar walk.
+__device__ __forceinline__ void direct_sum_range(const float4 *__restrict__ pos, int64_t n, int first, int count,
+                                                 float4 me, float eps2, float &fx, float &fy, float &fz,
+                                                 unsigned long long &n_pairs, bool count_pairs) {
+    const int q0 = first < 0 ? 0 : first;
+    const int q1 = first + count < n ? first + count : static_cast<int>(n);
+    for (int q = q0; q < q1; ++q) {
+        const float4 o = pos[q];
+        const float ex = __fsub_rn(o.x, me.x), ey = __fsub_rn(o.y, me.y), ez = __fsub_rn(o.z, me.z);
+        const float e2 = __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
+        if (o.w > 0.f && e2 > 0.f) {
+            if (count_pairs) ++n_pairs;
+            const float iv = rsqrt_ftz(e2 + eps2);
+            const float wq = o.w * iv * iv * iv;
+            fx = fmaf(ex, wq, fx);
+            fy = fmaf(ey, wq, fy);
+            fz = fmaf(ez, wq, fz);
+        }
+    }
+}
+
+__device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, float fy, float fz, float dt,
+                                                 float4 *__restrict__ pos_out, float4 *__restrict__ vel,
+                                                 float4 *__restrict__ acc, float4 *__restrict__ force_out,
+                                                 const int *__restrict__ ids, int64_t n) {
+    const float4 anew = make_float4(fx, fy, fz, 0.f);
+    if (pos_out) {
+        // Reference integrator (include/ParticleSystem.h:52-69), no contraction.
+        const float h = __fmul_rn(dt, 0.5f);
+        float4 v = vel[b];
+        const float4 a = acc[b];
+        v.x = __fadd_rn(v.x, __fmul_rn(a.x, h));
+        v.y = __fadd_rn(v.y, __fmul_rn(a.y, h));
+        v.z = __fadd_rn(v.z, __fmul_rn(a.z, h));
+        p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
+        p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+        p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
+        v.x = __fadd_rn(v.x, __fmul_rn(fx, h));
+        v.y = __fadd_rn(v.y, __fmul_rn(fy, h));
+        v.z = __fadd_rn(v.z, __fmul_rn(fz, h));
+        pos_out[b] = p;
+        vel[b] = v;
+        acc[b] = anew;
+    }
+    if (force_out) {
+        const int d = ids ? ids[b] : static_cast<int>(b);
+        if (d >= 0 && d < n) force_out[d] = anew;
+    }
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict__ nodes,
+                                                        const uint32_t *__restrict__ node_total,
+                                                        const float4 *__restrict__ pos, int64_t n, float eps2,
+                                                        float theta2, float dt, float4 *__restrict__ pos_out,
+                                                        float4 *__restrict__ vel, float4 *__restrict__ acc,
+                                                        float4 *__restrict__ force_out, const int *__restrict__ ids,
+                                                        unsigned long long *__restrict__ counters) {
+    unsigned long long n_pairs = 0, n_visits = 0;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t bA = warp * 64 + lane, bB = bA + 32;
+    const bool vA = bA < n, vB = bB < n;
+    const int m_nodes = static_cast<int>(*node_total);
+    const float4 meA = vA ? pos[bA] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 meB = vB ? pos[bB] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 nx = make_float2(-meA.x, -meB.x), ny = make_float2(-meA.y, -meB.y), nz = make_float2(-meA.z, -meB.z);
+    const float2 th = make_float2(theta2, theta2);
+    int skipA = vA ? 0 : m_nodes, skipB = vB ? 0 : m_nodes;
+    float fAx = 0.f, fAy = 0.f, fAz = 0.f, fBx = 0.f, fBy = 0.f, fBz = 0.f;
+    int i = 0;
+    while (i < m_nodes) {
+        const float4 cm = __ldg(&nodes[i].cm);
+        const int4 meta = __ldg(&nodes[i].meta);
+        const bool actA = skipA <= i, actB = skipB <= i;
+        const float2 dx = __fadd2_rn(make_float2(cm.x, cm.x), nx);
+        const float2 dy = __fadd2_rn(make_float2(cm.y, cm.y), ny);
+        const float2 dz = __fadd2_rn(make_float2(cm.z, cm.z), nz);
+        const float2 d2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
+        const float s2 = __int_as_float(meta.x);
+        const float2 rhs = __fmul2_rn(th, d2);
+        const bool accA = actA && (s2 < 0.f || s2 < rhs.x);
+        const bool accB = actB && (s2 < 0.f || s2 < rhs.y);
+        const bool self = meta.w <= 1 && cm.w > 0.f;
+        const bool useA = accA && self && d2.x > 0.f, useB = accB && self && d2.y > 0.f;
+        if (useA || useB) {
+            if (COUNT) n_pairs += (useA ? 1u : 0u) + (useB ? 1u : 0u);
+            const float2 e = make_float2(d2.x + eps2, d2.y + eps2);
+            const float2 inv = make_float2(rsqrt_ftz(e.x), rsqrt_ftz(e.y));
+            const float2 inv3 = __fmul2_rn(__fmul2_rn(inv, inv), inv);
+            const float2 w = make_float2(useA ? cm.w * inv3.x : 0.f, useB ? cm.w * inv3.y : 0.f);
+            fAx = fmaf(dx.x, w.x, fAx);
+            fAy = fmaf(dy.x, w.x, fAy);
+            fAz = fmaf(dz.x, w.x, fAz);
+            fBx = fmaf(dx.y, w.y, fBx);
+            fBy = fmaf(dy.y, w.y, fBy);
+            fBz = fmaf(dz.y, w.y, fBz);
+        }
+        if (meta.w != 0 && meta.w != 1) {  // warp-uniform: a bucket or a terminal cell
+            const int cntb = meta.w >= 2 ? meta.w : -meta.w;
+            if ((meta.w >= 2 && accA) || (meta.w < 0 && actA && !accA))
+                direct_sum_range(pos, n, meta.z, cntb, meA, eps2, fAx, fAy, fAz, n_pairs, COUNT);
+            if ((meta.w >= 2 && accB) || (meta.w < 0 && actB && !accB))
+                direct_sum_range(pos, n, meta.z, cntb, meB, eps2, fBx, fBy, fBz, n_pairs, COUNT);
+        }
+        const bool doneA = accA || (actA && meta.w < 0), doneB = accB || (actB && meta.w < 0);
+        if (doneA) skipA = meta.y;
+        if (doneB) skipB = meta.y;
+        const bool open = (actA && !doneA) || (actB && !doneB);
+        if (COUNT) ++n_visits;
+        if (__any_sync(0xffffffffu, open)) {
+            ++i;
+        } else {
+            const int mine = skipA < skipB ? skipA : skipB;
+            const int nx2 = static_cast<int>(__reduce_min_sync(0xffffffffu, static_cast<unsigned>(mine)));
+            i = nx2 > i ? nx2 : i + 1;
+        }
+    }
+    if (COUNT) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) n_pairs += __shfl_down_sync(0xffffffffu, n_pairs, off);
+        if (lane == 0) {
+            atomicAdd(&counters[0], n_pairs);
+            atomicAdd(&counters[1], n_visits);
+        }
+    }
+    if (vA) integrate_sorted(bA, meA, fAx, fAy, fAz, dt, pos_out, vel, acc, force_out, ids, n);
+    if (vB) integrate_sorted(bB, meB, fBx, fBy, fBz, dt, pos_out, vel, acc, force_out, ids, n);
+}
+
 // out[ids[i]] = in[i] (back to the caller's body order), positions with w = 0.
 __global__ void unpermute_kernel(const int *__restrict__ ids, int64_t n, const float4 *__restrict__ in,
                                  float4 *__restrict__ out, int zero_w, int *status) {
@@ -826,7 +959,16 @@ cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &
                         cudaStream_t st, StageTimer *timer) {
     if (timer) timer->begin(kStageTraverse, st);
     // The record count P[n] stays on the device; the kernel reads it.
-    if (w.counters)
+    if (w.bodies_per_lane == 2) {
+        const int64_t warps = (n + 63) / 64;
+        const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
+        if (w.counters)
+            traverse2_kernel<true><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out,
+                                                           vel, acc, force_out, ids, w.counters);
+        else
+            traverse2_kernel<false><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out,
+                                                            vel, acc, force_out, ids, nullptr);
+    } else if (w.counters)
         traverse_kernel<true><<<grid_for(n, 256), 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
                                                                 pos_out, vel, acc, force_out, ids, w.counters);
     else

@@ -53,6 +53,7 @@ struct BHWorkspace {
     // traversal counts into `counters` when it is set (= counter_mem).
     unsigned long long *counter_mem = nullptr;
     unsigned long long *counters = nullptr;
+    int bodies_per_lane = 1;  // traversal shape: 1 or 2 bodies per lane
     int64_t node_count_host = 0;
 };
 

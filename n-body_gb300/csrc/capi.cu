@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -198,6 +199,12 @@ int ensure_workspace(nbody_ctx *ctx, int64_t n) {
     const bool counting = ctx->ws.counters != nullptr;
     nbody::bh_workspace_layout(n, ctx->ws_mem, &ctx->ws);
     if (counting) ctx->ws.counters = ctx->ws.counter_mem;
+    // Two bodies per lane measured faster at N = 2^20 (Plummer): 62M instead
+    // of 110M warp record visits per step, traversal 5.95 ms instead of 7.12 ms.
+    ctx->ws.bodies_per_lane = 2;
+    if (const char *e = std::getenv("NBODY_BH_BODIES_PER_LANE")) {
+        if (std::atoi(e) == 1) ctx->ws.bodies_per_lane = 1;
+    }
     return NBODY_OK;
 }
 
