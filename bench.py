@@ -9,6 +9,10 @@ no public dataset is involved):
        theta = 0.5, eps^2 = 40, dt = 0.0035 (the reference's -v 6 path).
        Metric: body-steps/s. The line also carries a "pp" object with the
        direct-sum workload measured the same way.
+  discs: Barnes-Hut at scale, N = 2^24: two exponential discs of 8,388,607
+       bodies (scale length 200, sech^2 height 20, circular velocities) plus a
+       1e6 point mass each, 2,000 apart at relative speed 50, inclined 30 deg;
+       theta = 0.6, eps^2 = 40, dt = 0.0035 (5 steps by default).
   pp : direct sum, N = 16,384 bodies uniform in a ball of radius 100, masses
        U[1, 10), v = 0, dt = 0.0035, eps^2 = 40 (the reference's -v 2 path).
        Metric: interactions/s (N^2 per step, 20 flop each by convention).
@@ -47,6 +51,7 @@ import numpy as np  # noqa: E402
 METRIC = "PP interactions/s (%FP32 peak), BH body-steps/s; served sims/s + p99 vs plain"
 PP_N, PP_DT, PP_EPS2 = 16384, 0.0035, 40.0
 BH_N, BH_DT, BH_EPS2, BH_THETA2 = 1 << 20, 0.0035, 40.0, 0.25
+DISCS_THETA2 = 0.36  # theta = 0.6
 # Algorithmic bytes per body per step of the HBM-bound Barnes-Hut stages:
 # bbox reads pos (16); keys read pos, write key + index (16 + 12); the sort reads
 # keys once for the histograms (8) and moves key + index in and out in 8 passes
@@ -295,10 +300,16 @@ def bench_bh(args, world, rank, local, dist):
     from nbody_gb300 import initializers as I
 
     torch.cuda.set_device(local)
-    n = BH_N
-    pos, vel, mass = I.plummer(n, a=100.0, seed=12345 + rank)
+    discs = args.workload == "discs"
+    if discs:
+        pos, vel, mass = I.two_discs(seed=12345 + rank)
+        theta2 = DISCS_THETA2
+    else:
+        pos, vel, mass = I.plummer(BH_N, a=100.0, seed=12345 + rank)
+        theta2 = BH_THETA2
+    n = len(mass)
     system = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
-    solver = nb.ParticleSolverCUDA(BH_DT, BH_EPS2, n, mode="bh", theta2=BH_THETA2, device=local)
+    solver = nb.ParticleSolverCUDA(BH_DT, BH_EPS2, n, mode="bh", theta2=theta2, device=local)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     solver.set_stream(stream.cuda_stream)
@@ -393,12 +404,16 @@ def bench_bh(args, world, rank, local, dist):
     line = {"metric": METRIC, "component": "BH body-steps/s", "value": value, "unit": "body-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "Barnes-Hut, N=1048576 equal-mass Plummer sphere a=100 (truncated at 20a, "
-                                   "velocities from the Plummer DF), theta=0.5, eps2=40, dt=0.0035 "
-                                   "(reference -v 6 path)", "n_bodies": n, "parallelism": "replicas",
+            "config": {"workload": ("Barnes-Hut at scale, N=16777216: two exponential discs of 8388607 bodies "
+                                    "(m=1, scale length 200, sech^2 height 20, circular velocities) + a 1e6 point "
+                                    "mass each, 2000 apart, relative speed 50, inclined 30 deg; theta=0.6, eps2=40, "
+                                    "dt=0.0035 (reference -v 6 path)") if discs else
+                                   ("Barnes-Hut, N=1048576 equal-mass Plummer sphere a=100 (truncated at 20a, "
+                                    "velocities from the Plummer DF), theta=0.5, eps2=40, dt=0.0035 "
+                                    "(reference -v 6 path)"), "n_bodies": n, "parallelism": "replicas",
                        "l2": "flushed between steps (256 MiB write, outside the event pair)"},
             "clocks": clocks, "roofline": roofline, "e2e": e2e, "gpu_launches": launches_per_step * args.steps}
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and not discs:
         line["cpu_baseline"] = cpu_baseline_bh()
     solver.close()
     torch.cuda.set_stream(torch.cuda.default_stream())
@@ -514,7 +529,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", choices=["bh", "pp"], default="bh")
+    ap.add_argument("--workload", choices=["bh", "discs", "pp"], default="bh")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-pp", action="store_true", help="leave the nested direct-sum measurement out")
@@ -536,7 +551,7 @@ def main():
         line = bench_pp(args, world, rank, local, dist)
     else:
         line = bench_bh(args, world, rank, local, dist)
-        if not args.no_pp:
+        if not args.no_pp and args.workload == "bh":
             pp_args = argparse.Namespace(**vars(args))
             pp_args.steps = 100
             pp = bench_pp(pp_args, world, rank, local, dist)

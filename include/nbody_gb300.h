@@ -123,6 +123,14 @@ int nbody_pp_step_device(nbody_ctx *ctx, const void *pos_in, void *pos_out, void
  * thread, j-slices and CTAs. For tests and tuning reports. */
 int nbody_pp_config(nbody_ctx *ctx, int64_t n, int *bodies_per_thread, int *slices, int *ctas);
 
+/* Conservation diagnostics of the resident state, computed in FP64 (the only
+ * FP64 arithmetic on the GPU; the reference has no diagnostics): out[0]
+ * kinetic energy, out[1] potential energy (softened, each pair once; direct sum
+ * for a PP context, the Barnes-Hut walk with the context's theta2 for a BH
+ * context), out[2..4] linear momentum, out[5..7] angular momentum about the
+ * origin. Waits for the context's stream. */
+int nbody_diagnostics(nbody_ctx *ctx, double *out);
+
 /* Selects the key used to build the Barnes-Hut tree (NBODY_KEYS_*). */
 int nbody_set_key_mode(nbody_ctx *ctx, int mode);
 

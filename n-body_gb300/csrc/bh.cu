@@ -584,7 +584,8 @@ __global__ void __launch_bounds__(256) traverse_kernel(const BHNode *__restrict_
 // f32x2 arithmetic, each lane of a pair rounded exactly as the scalar walk.
 __device__ __forceinline__ void direct_sum_range(const float4 *__restrict__ pos, int64_t n, int first, int count,
                                                  float4 me, float eps2, float &fx, float &fy, float &fz,
-                                                 unsigned long long &n_pairs, bool count_pairs) {
+                                                 unsigned long long &n_pairs, bool count_pairs, float &phi,
+                                                 bool pot) {
     const int q0 = first < 0 ? 0 : first;
     const int q1 = first + count < n ? first + count : static_cast<int>(n);
     for (int q = q0; q < q1; ++q) {
@@ -598,6 +599,7 @@ __device__ __forceinline__ void direct_sum_range(const float4 *__restrict__ pos,
             fx = fmaf(ex, wq, fx);
             fy = fmaf(ey, wq, fy);
             fz = fmaf(ez, wq, fz);
+            if (pot) phi = fmaf(-o.w, iv, phi);
         }
     }
 }
@@ -631,15 +633,19 @@ __device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, 
     }
 }
 
-template <bool COUNT>
+// POT also accumulates the potential -sum m / sqrt(d^2 + eps^2) over the same
+// accepted records (for the energy diagnostic) into phi_out[ids[b]].
+template <bool COUNT, bool POT>
 __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict__ nodes,
                                                         const uint32_t *__restrict__ node_total,
                                                         const float4 *__restrict__ pos, int64_t n, float eps2,
                                                         float theta2, float dt, float4 *__restrict__ pos_out,
                                                         float4 *__restrict__ vel, float4 *__restrict__ acc,
                                                         float4 *__restrict__ force_out, const int *__restrict__ ids,
-                                                        unsigned long long *__restrict__ counters) {
+                                                        unsigned long long *__restrict__ counters,
+                                                        float *__restrict__ phi_out) {
     unsigned long long n_pairs = 0, n_visits = 0;
+    float phiA = 0.f, phiB = 0.f;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t bA = warp * 64 + lane, bB = bA + 32;
@@ -678,13 +684,17 @@ __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict
             fBx = fmaf(dx.y, w.y, fBx);
             fBy = fmaf(dy.y, w.y, fBy);
             fBz = fmaf(dz.y, w.y, fBz);
+            if (POT) {
+                phiA = fmaf(useA ? -cm.w : 0.f, inv.x, phiA);
+                phiB = fmaf(useB ? -cm.w : 0.f, inv.y, phiB);
+            }
         }
         if (meta.w != 0 && meta.w != 1) {  // warp-uniform: a bucket or a terminal cell
             const int cntb = meta.w >= 2 ? meta.w : -meta.w;
             if ((meta.w >= 2 && accA) || (meta.w < 0 && actA && !accA))
-                direct_sum_range(pos, n, meta.z, cntb, meA, eps2, fAx, fAy, fAz, n_pairs, COUNT);
+                direct_sum_range(pos, n, meta.z, cntb, meA, eps2, fAx, fAy, fAz, n_pairs, COUNT, phiA, POT);
             if ((meta.w >= 2 && accB) || (meta.w < 0 && actB && !accB))
-                direct_sum_range(pos, n, meta.z, cntb, meB, eps2, fBx, fBy, fBz, n_pairs, COUNT);
+                direct_sum_range(pos, n, meta.z, cntb, meB, eps2, fBx, fBy, fBz, n_pairs, COUNT, phiB, POT);
         }
         const bool doneA = accA || (actA && meta.w < 0), doneB = accB || (actB && meta.w < 0);
         if (doneA) skipA = meta.y;
@@ -706,6 +716,17 @@ __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict
             atomicAdd(&counters[0], n_pairs);
             atomicAdd(&counters[1], n_visits);
         }
+    }
+    if (POT) {
+        if (vA) {
+            const int d = ids ? ids[bA] : static_cast<int>(bA);
+            if (d >= 0 && d < n) phi_out[d] = phiA;
+        }
+        if (vB) {
+            const int d = ids ? ids[bB] : static_cast<int>(bB);
+            if (d >= 0 && d < n) phi_out[d] = phiB;
+        }
+        return;
     }
     if (vA) integrate_sorted(bA, meA, fAx, fAy, fAz, dt, pos_out, vel, acc, force_out, ids, n);
     if (vB) integrate_sorted(bB, meB, fBx, fBy, fBz, dt, pos_out, vel, acc, force_out, ids, n);
@@ -963,11 +984,13 @@ cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &
         const int64_t warps = (n + 63) / 64;
         const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
         if (w.counters)
-            traverse2_kernel<true><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out,
-                                                           vel, acc, force_out, ids, w.counters);
+            traverse2_kernel<true, false><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
+                                                                  pos_out, vel, acc, force_out, ids, w.counters,
+                                                                  nullptr);
         else
-            traverse2_kernel<false><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out,
-                                                            vel, acc, force_out, ids, nullptr);
+            traverse2_kernel<false, false><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
+                                                                   pos_out, vel, acc, force_out, ids, nullptr,
+                                                                   nullptr);
     } else if (w.counters)
         traverse_kernel<true><<<grid_for(n, 256), 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
                                                                 pos_out, vel, acc, force_out, ids, w.counters);
@@ -975,6 +998,15 @@ cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &
         traverse_kernel<false><<<grid_for(n, 256), 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
                                                                  pos_out, vel, acc, force_out, ids, nullptr);
     if (timer) timer->end(kStageTraverse, st);
+    return cudaGetLastError();
+}
+
+cudaError_t bh_potential(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,
+                         float *phi_out, const int *ids, cudaStream_t st) {
+    const int64_t warps = (n + 63) / 64;
+    const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
+    traverse2_kernel<false, true><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, 0.f, nullptr,
+                                                          nullptr, nullptr, nullptr, ids, nullptr, phi_out);
     return cudaGetLastError();
 }
 

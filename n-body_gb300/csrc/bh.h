@@ -78,6 +78,10 @@ cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaSt
 cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,
                         float dt, float4 *pos_out, float4 *vel, float4 *acc, float4 *force_out, const int *ids,
                         cudaStream_t st, StageTimer *timer);
+// Potential -sum m / sqrt(d^2 + eps^2) of every sorted body over the same
+// accepted records as the forces, into phi_out[ids[b]] (or phi_out[b]).
+cudaError_t bh_potential(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,
+                         float *phi_out, const int *ids, cudaStream_t st);
 cudaError_t bh_unpermute(const int *ids, int64_t n, const float4 *in, float4 *out, bool zero_w, cudaStream_t st,
                          int *status);
 

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "bh.h"
+#include "diag.h"
 #include "kernels.h"
 #include "nbody_gb300.h"
 #include "sort.h"
@@ -111,6 +112,9 @@ struct nbody_ctx {
     float4 *dev_pos = nullptr;
     int *dev_ids = nullptr;
     int64_t dev_cap = 0;
+    // Diagnostics: reduction scratch, 8 doubles of output, per-body potential.
+    void *diag_mem = nullptr;
+    float *diag_phi = nullptr;
 };
 
 namespace {
@@ -182,6 +186,20 @@ int pp_steps(nbody_ctx *ctx, int steps) {
                                     ctx->status, ctx->timer));
         ctx->cur ^= 1;
     }
+    return NBODY_OK;
+}
+
+int ensure_dev_buffers(nbody_ctx *ctx, int64_t n) {
+    if (ctx->dev_cap >= n) return NBODY_OK;
+    NB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->dev_pos);
+    cudaFree(ctx->dev_ids);
+    ctx->dev_pos = nullptr;
+    ctx->dev_ids = nullptr;
+    ctx->dev_cap = 0;
+    NB_CK(ctx, cudaMalloc(&ctx->dev_pos, sizeof(float4) * static_cast<size_t>(n)));
+    NB_CK(ctx, cudaMalloc(&ctx->dev_ids, sizeof(int) * static_cast<size_t>(n)));
+    ctx->dev_cap = n;
     return NBODY_OK;
 }
 
@@ -330,6 +348,8 @@ int nbody_destroy(nbody_ctx *ctx) {
         cudaFree(ctx->ws_mem);
         cudaFree(ctx->dev_pos);
         cudaFree(ctx->dev_ids);
+        cudaFree(ctx->diag_mem);
+        cudaFree(ctx->diag_phi);
         delete ctx->timer;
         if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     }
@@ -485,18 +505,8 @@ int nbody_bh_forces_device(nbody_ctx *ctx, const void *pos_mass4, void *force4, 
         return NBODY_ERR_ARG;
     DeviceGuard dg(ctx->device);
     int rc = ensure_workspace(ctx, n);
+    if (rc == NBODY_OK) rc = ensure_dev_buffers(ctx, n);
     if (rc != NBODY_OK) return rc;
-    if (ctx->dev_cap < n) {
-        NB_CK(ctx, cudaStreamSynchronize(ctx->stream));
-        cudaFree(ctx->dev_pos);
-        cudaFree(ctx->dev_ids);
-        ctx->dev_pos = nullptr;
-        ctx->dev_ids = nullptr;
-        ctx->dev_cap = 0;
-        NB_CK(ctx, cudaMalloc(&ctx->dev_pos, sizeof(float4) * static_cast<size_t>(n)));
-        NB_CK(ctx, cudaMalloc(&ctx->dev_ids, sizeof(int) * static_cast<size_t>(n)));
-        ctx->dev_cap = n;
-    }
     nbody::BHWorkspace &w = ctx->ws;
     const float4 *p = static_cast<const float4 *>(pos_mass4);
     nbody::StageTimer *tm = ctx->timer;
@@ -616,6 +626,45 @@ int nbody_profile_read(nbody_ctx *ctx, double *ms, int *launches, int nstages) {
     DeviceGuard dg(ctx->device);
     NB_CK(ctx, ctx->timer->read(ms, launches, nstages));
     return NBODY_OK;
+}
+
+int nbody_diagnostics(nbody_ctx *ctx, double *out) {
+    if (!ctx || !out) return NBODY_ERR_ARG;
+    if (!ctx->uploaded) return NBODY_ERR_STATE;
+    DeviceGuard dg(ctx->device);
+    const int64_t n = ctx->n;
+    if (!ctx->diag_mem) {
+        NB_CK(ctx, cudaMalloc(&ctx->diag_mem, nbody::diag_scratch_bytes() + 256));
+        NB_CK(ctx, cudaMemsetAsync(ctx->diag_mem, 0, nbody::diag_scratch_bytes() + 256, ctx->stream));
+        NB_CK(ctx, cudaMalloc(&ctx->diag_phi, sizeof(float) * static_cast<size_t>(n)));
+    }
+    double *out_dev = reinterpret_cast<double *>(static_cast<char *>(ctx->diag_mem) + nbody::diag_scratch_bytes());
+    const float4 *P, *V;
+    if (ctx->mode == NBODY_MODE_PP) {
+        P = ctx->pos[ctx->cur];
+        V = ctx->vel;
+        NB_CK(ctx, nbody::diag_pp_potential(P, n, ctx->eps2, ctx->diag_phi, ctx->stream));
+    } else {
+        // A tree over the current positions (the last step's tree predates the
+        // integrator), built on copies so that the resident order is kept.
+        P = ctx->pos[ctx->bh_pos];
+        V = ctx->vel2[ctx->bh_va];
+        int rc = ensure_workspace(ctx, n);
+        if (rc == NBODY_OK) rc = ensure_dev_buffers(ctx, n);
+        if (rc != NBODY_OK) return rc;
+        nbody::BHWorkspace &w = ctx->ws;
+        NB_CK(ctx, nbody::bh_bbox(P, n, w, ctx->stream, nullptr));
+        NB_CK(ctx, nbody::bh_keys(P, n, w, ctx->key_mode, ctx->stream, nullptr));
+        NB_CK(ctx, nbody::bh_sort(n, w, ctx->stream, ctx->status, nullptr));
+        NB_CK(ctx, nbody::bh_gather(n, w, P, nullptr, nullptr, nullptr, ctx->dev_pos, nullptr, nullptr, ctx->dev_ids,
+                                    ctx->stream, ctx->status, nullptr));
+        NB_CK(ctx, nbody::bh_build(ctx->dev_pos, n, w, ctx->stream, ctx->status, nullptr));
+        NB_CK(ctx, nbody::bh_potential(ctx->dev_pos, n, w, ctx->eps2, ctx->theta2, ctx->diag_phi, ctx->dev_ids,
+                                       ctx->stream));
+    }
+    NB_CK(ctx, nbody::diag_momenta(P, V, ctx->diag_phi, n, ctx->diag_mem, out_dev, ctx->stream));
+    NB_CK(ctx, cudaMemcpyAsync(out, out_dev, sizeof(double) * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    return read_status(ctx);
 }
 
 int nbody_set_key_mode(nbody_ctx *ctx, int mode) {

@@ -66,6 +66,7 @@ SIGNATURES = {
     "nbody_bh_tree_export": (_i, [_vp, _vp, _i64, ctypes.POINTER(_i64), _vp]),
     "nbody_bh_counters": (_i, [_vp, _i, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "nbody_set_key_mode": (_i, [_vp, _i]),
+    "nbody_diagnostics": (_i, [_vp, ctypes.POINTER(ctypes.c_double)]),
 }
 
 
@@ -278,6 +279,14 @@ class ParticleSolverCUDA:
                     "nbody_bh_tree_export")
         rec = rec[:m]
         return rec[:, :4].copy(), rec[:, 4:].view(np.int32).copy(), box
+
+    def diagnostics(self) -> dict:
+        """FP64 kinetic/potential energy, linear and angular momentum of the resident state."""
+        out = (ctypes.c_double * 8)()
+        self._check(lib().nbody_diagnostics(self._ctx, out), "nbody_diagnostics")
+        v = list(out)
+        return {"kinetic": v[0], "potential": v[1], "energy": v[0] + v[1], "momentum": v[2:5],
+                "angular_momentum": v[5:8]}
 
     def set_key_mode(self, mode) -> None:
         """'octree' (the reference's FP32 cell descent, default) or 'morton' (morton.glsl quantisation)."""
