@@ -59,6 +59,17 @@ extern "C" {
 #define NBODY_KEYS_OCTREE 0
 #define NBODY_KEYS_MORTON 1
 
+/* Integrator applied after the forces of each step:
+ * NBODY_INTEGRATOR_CPU (default): the reference's CPU order
+ *   (ParticleSystem::updateParticlePosition, include/ParticleSystem.h:52-69):
+ *   v += a dt/2; x += v dt; a = F; v += a dt/2.
+ * NBODY_INTEGRATOR_GPU_EULER: the reference's GLSL path
+ *   (src/shaders/ComputeShaders/updateParticles.glsl:44-55): v += F dt; x += v dt.
+ *   The accelerations array then holds F (the forces output), which the GLSL
+ *   path leaves untouched. Every operation is rounded on its own. */
+#define NBODY_INTEGRATOR_CPU 0
+#define NBODY_INTEGRATOR_GPU_EULER 1
+
 typedef struct nbody_ctx nbody_ctx;
 
 /* Human-readable name of a status code. */
@@ -130,6 +141,9 @@ int nbody_pp_config(nbody_ctx *ctx, int64_t n, int *bodies_per_thread, int *slic
  * context), out[2..4] linear momentum, out[5..7] angular momentum about the
  * origin. Waits for the context's stream. */
 int nbody_diagnostics(nbody_ctx *ctx, double *out);
+
+/* Selects the integrator (NBODY_INTEGRATOR_*). */
+int nbody_set_integrator(nbody_ctx *ctx, int integrator);
 
 /* Selects the key used to build the Barnes-Hut tree (NBODY_KEYS_*). */
 int nbody_set_key_mode(nbody_ctx *ctx, int mode);

@@ -467,6 +467,11 @@ __global__ void upsweep_kernel(const uint64_t *__restrict__ k, int64_t n, const 
 // the record's `next`. The warp descends (i + 1) if any lane opened the
 // record, otherwise it jumps to the smallest `skip` of its lanes. Every lane
 // therefore sees exactly the records its own reference walk would accept.
+__device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, float fy, float fz, float dt,
+                                                 float4 *__restrict__ pos_out, float4 *__restrict__ vel,
+                                                 float4 *__restrict__ acc, float4 *__restrict__ force_out,
+                                                 const int *__restrict__ ids, int64_t n, int euler);
+
 // COUNT adds up (per warp, one atomic each) the pairwise force evaluations
 // and the records the warp visited; used for measurement only.
 template <bool COUNT>
@@ -476,7 +481,7 @@ __global__ void __launch_bounds__(256) traverse_kernel(const BHNode *__restrict_
                                                        float theta2, float dt, float4 *__restrict__ pos_out,
                                                        float4 *__restrict__ vel, float4 *__restrict__ acc,
                                                        float4 *__restrict__ force_out, const int *__restrict__ ids,
-                                                       unsigned long long *__restrict__ counters) {
+                                                       unsigned long long *__restrict__ counters, int euler) {
     unsigned long long n_pairs = 0, n_visits = 0;
     const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const bool valid = b < n;
@@ -552,30 +557,7 @@ __global__ void __launch_bounds__(256) traverse_kernel(const BHNode *__restrict_
         }
     }
     if (!valid) return;
-    const float4 anew = make_float4(fx, fy, fz, 0.f);
-    if (pos_out) {
-        // Reference integrator (include/ParticleSystem.h:52-69), no contraction.
-        const float h = __fmul_rn(dt, 0.5f);
-        float4 v = vel[b];
-        const float4 a = acc[b];
-        float4 p = me;
-        v.x = __fadd_rn(v.x, __fmul_rn(a.x, h));
-        v.y = __fadd_rn(v.y, __fmul_rn(a.y, h));
-        v.z = __fadd_rn(v.z, __fmul_rn(a.z, h));
-        p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
-        p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
-        p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
-        v.x = __fadd_rn(v.x, __fmul_rn(fx, h));
-        v.y = __fadd_rn(v.y, __fmul_rn(fy, h));
-        v.z = __fadd_rn(v.z, __fmul_rn(fz, h));
-        pos_out[b] = p;
-        vel[b] = v;
-        acc[b] = anew;
-    }
-    if (force_out) {
-        const int d = ids ? ids[b] : static_cast<int>(b);
-        if (d >= 0 && d < n) force_out[d] = anew;
-    }
+    integrate_sorted(b, me, fx, fy, fz, dt, pos_out, vel, acc, force_out, ids, n, euler);
 }
 
 // Two bodies per lane: a warp serves 64 consecutive sorted bodies (lane l
@@ -607,9 +589,21 @@ __device__ __forceinline__ void direct_sum_range(const float4 *__restrict__ pos,
 __device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, float fy, float fz, float dt,
                                                  float4 *__restrict__ pos_out, float4 *__restrict__ vel,
                                                  float4 *__restrict__ acc, float4 *__restrict__ force_out,
-                                                 const int *__restrict__ ids, int64_t n) {
+                                                 const int *__restrict__ ids, int64_t n, int euler) {
     const float4 anew = make_float4(fx, fy, fz, 0.f);
-    if (pos_out) {
+    if (pos_out && euler) {
+        // updateParticles.glsl:44-55: v += F dt, then x += v dt.
+        float4 v = vel[b];
+        v.x = __fadd_rn(v.x, __fmul_rn(fx, dt));
+        v.y = __fadd_rn(v.y, __fmul_rn(fy, dt));
+        v.z = __fadd_rn(v.z, __fmul_rn(fz, dt));
+        p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
+        p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+        p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
+        pos_out[b] = p;
+        vel[b] = v;
+        acc[b] = anew;
+    } else if (pos_out) {
         // Reference integrator (include/ParticleSystem.h:52-69), no contraction.
         const float h = __fmul_rn(dt, 0.5f);
         float4 v = vel[b];
@@ -643,7 +637,7 @@ __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict
                                                         float4 *__restrict__ vel, float4 *__restrict__ acc,
                                                         float4 *__restrict__ force_out, const int *__restrict__ ids,
                                                         unsigned long long *__restrict__ counters,
-                                                        float *__restrict__ phi_out) {
+                                                        float *__restrict__ phi_out, int euler) {
     unsigned long long n_pairs = 0, n_visits = 0;
     float phiA = 0.f, phiB = 0.f;
     const int lane = threadIdx.x & 31;
@@ -728,8 +722,8 @@ __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict
         }
         return;
     }
-    if (vA) integrate_sorted(bA, meA, fAx, fAy, fAz, dt, pos_out, vel, acc, force_out, ids, n);
-    if (vB) integrate_sorted(bB, meB, fBx, fBy, fBz, dt, pos_out, vel, acc, force_out, ids, n);
+    if (vA) integrate_sorted(bA, meA, fAx, fAy, fAz, dt, pos_out, vel, acc, force_out, ids, n, euler);
+    if (vB) integrate_sorted(bB, meB, fBx, fBy, fBz, dt, pos_out, vel, acc, force_out, ids, n, euler);
 }
 
 // out[ids[i]] = in[i] (back to the caller's body order), positions with w = 0.
@@ -977,7 +971,7 @@ cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaSt
 
 cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,
                         float dt, float4 *pos_out, float4 *vel, float4 *acc, float4 *force_out, const int *ids,
-                        cudaStream_t st, StageTimer *timer) {
+                        int euler, cudaStream_t st, StageTimer *timer) {
     if (timer) timer->begin(kStageTraverse, st);
     // The record count P[n] stays on the device; the kernel reads it.
     if (w.bodies_per_lane == 2) {
@@ -986,17 +980,17 @@ cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &
         if (w.counters)
             traverse2_kernel<true, false><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
                                                                   pos_out, vel, acc, force_out, ids, w.counters,
-                                                                  nullptr);
+                                                                  nullptr, euler);
         else
             traverse2_kernel<false, false><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
                                                                    pos_out, vel, acc, force_out, ids, nullptr,
-                                                                   nullptr);
+                                                                   nullptr, euler);
     } else if (w.counters)
         traverse_kernel<true><<<grid_for(n, 256), 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
-                                                                pos_out, vel, acc, force_out, ids, w.counters);
+                                                                pos_out, vel, acc, force_out, ids, w.counters, euler);
     else
         traverse_kernel<false><<<grid_for(n, 256), 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
-                                                                 pos_out, vel, acc, force_out, ids, nullptr);
+                                                                 pos_out, vel, acc, force_out, ids, nullptr, euler);
     if (timer) timer->end(kStageTraverse, st);
     return cudaGetLastError();
 }
@@ -1006,7 +1000,7 @@ cudaError_t bh_potential(const float4 *pos_sorted, int64_t n, const BHWorkspace 
     const int64_t warps = (n + 63) / 64;
     const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
     traverse2_kernel<false, true><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, 0.f, nullptr,
-                                                          nullptr, nullptr, nullptr, ids, nullptr, phi_out);
+                                                          nullptr, nullptr, nullptr, ids, nullptr, phi_out, 0);
     return cudaGetLastError();
 }
 

@@ -75,9 +75,10 @@ cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaSt
 // Forces for every sorted body; with pos_out set, also the reference
 // integrator (pos_out must not alias pos_sorted). force_out, if set, receives
 // the acceleration at index ids[b] (or b when ids is null).
+// euler = 1 applies the GLSL path's semi-implicit Euler instead of the CPU order.
 cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,
                         float dt, float4 *pos_out, float4 *vel, float4 *acc, float4 *force_out, const int *ids,
-                        cudaStream_t st, StageTimer *timer);
+                        int euler, cudaStream_t st, StageTimer *timer);
 // Potential -sum m / sqrt(d^2 + eps^2) of every sorted body over the same
 // accepted records as the forces, into phi_out[ids[b]] (or phi_out[b]).
 cudaError_t bh_potential(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,

@@ -103,6 +103,7 @@ struct nbody_ctx {
     int *ids[2] = {nullptr, nullptr};
     int bh_pos = 0, bh_va = 0;
     int key_mode = NBODY_KEYS_OCTREE;
+    int integrator = NBODY_INTEGRATOR_CPU;
     bool ids_valid = false;  // false until the first step after an upload
     // Barnes-Hut workspace (keys, sort scratch, tree), grown on demand.
     void *ws_mem = nullptr;
@@ -182,6 +183,7 @@ int pp_steps(nbody_ctx *ctx, int steps) {
         g.vel = ctx->vel;
         g.acc = ctx->acc;
         g.dt = ctx->dt;
+        g.euler = ctx->integrator == NBODY_INTEGRATOR_GPU_EULER;
         NB_CK(ctx, nbody::pp_launch(plan, ctx->pos[ctx->cur], ctx->n, ctx->eps2, g, ctx->scratch, ctx->stream,
                                     ctx->status, ctx->timer));
         ctx->cur ^= 1;
@@ -243,7 +245,7 @@ int bh_step(nbody_ctx *ctx) {
     NB_CK(ctx, nbody::bh_build(Po, n, w, ctx->stream, ctx->status, tm));
     // New positions go to the buffer the gather just read from.
     NB_CK(ctx, nbody::bh_traverse(Po, n, w, ctx->eps2, ctx->theta2, ctx->dt, P, Vo, Ao, nullptr, nullptr,
-                                  ctx->stream, tm));
+                                  ctx->integrator == NBODY_INTEGRATOR_GPU_EULER, ctx->stream, tm));
     ctx->bh_va ^= 1;
     ctx->ids_valid = true;
     return NBODY_OK;
@@ -517,7 +519,7 @@ int nbody_bh_forces_device(nbody_ctx *ctx, const void *pos_mass4, void *force4, 
                                 ctx->stream, ctx->status, tm));
     NB_CK(ctx, nbody::bh_build(ctx->dev_pos, n, w, ctx->stream, ctx->status, tm));
     NB_CK(ctx, nbody::bh_traverse(ctx->dev_pos, n, w, ctx->eps2, ctx->theta2, 0.f, nullptr, nullptr, nullptr,
-                                  static_cast<float4 *>(force4), ctx->dev_ids, ctx->stream, tm));
+                                  static_cast<float4 *>(force4), ctx->dev_ids, 0, ctx->stream, tm));
     return NBODY_OK;
 }
 
@@ -570,6 +572,7 @@ int nbody_pp_step_device(nbody_ctx *ctx, const void *pos_in, void *pos_out, void
     g.acc = static_cast<float4 *>(acc4);
     g.force = static_cast<float4 *>(force4);
     g.dt = ctx->dt;
+    g.euler = ctx->integrator == NBODY_INTEGRATOR_GPU_EULER;
     NB_CK(ctx, nbody::pp_launch(plan, static_cast<const float4 *>(pos_in), n, ctx->eps2, g, ctx->scratch,
                                 ctx->stream, ctx->status, ctx->timer));
     return NBODY_OK;
@@ -665,6 +668,13 @@ int nbody_diagnostics(nbody_ctx *ctx, double *out) {
     NB_CK(ctx, nbody::diag_momenta(P, V, ctx->diag_phi, n, ctx->diag_mem, out_dev, ctx->stream));
     NB_CK(ctx, cudaMemcpyAsync(out, out_dev, sizeof(double) * 8, cudaMemcpyDeviceToHost, ctx->stream));
     return read_status(ctx);
+}
+
+int nbody_set_integrator(nbody_ctx *ctx, int integrator) {
+    if (!ctx || (integrator != NBODY_INTEGRATOR_CPU && integrator != NBODY_INTEGRATOR_GPU_EULER))
+        return NBODY_ERR_ARG;
+    ctx->integrator = integrator;
+    return NBODY_OK;
 }
 
 int nbody_set_key_mode(nbody_ctx *ctx, int mode) {

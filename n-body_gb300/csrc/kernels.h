@@ -14,6 +14,7 @@ struct Integrate {
     float4 *acc = nullptr;
     float4 *force = nullptr;  // optional copy of the new acceleration
     float dt = 0.f;
+    int euler = 0;  // 1: the GLSL path's semi-implicit Euler (updateParticles.glsl:44-55)
 };
 
 // Optional per-stage timing: when set, launchers record a CUDA event pair

@@ -43,6 +43,21 @@ __device__ __forceinline__ void integrate_body(int64_t i, float4 p, float fx, fl
     const float dt = g.dt;
     const float h = __fmul_rn(dt, 0.5f);
     float4 v = g.vel[i];
+    const float4 anew = make_float4(fx, fy, fz, 0.f);
+    if (g.euler) {
+        // updateParticles.glsl:44-55: v += F dt, then x += v dt.
+        v.x = __fadd_rn(v.x, __fmul_rn(fx, dt));
+        v.y = __fadd_rn(v.y, __fmul_rn(fy, dt));
+        v.z = __fadd_rn(v.z, __fmul_rn(fz, dt));
+        p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));
+        p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+        p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
+        g.pos_out[i] = p;
+        g.vel[i] = v;
+        g.acc[i] = anew;
+        if (g.force) g.force[i] = anew;
+        return;
+    }
     const float4 a = g.acc[i];
     v.x = __fadd_rn(v.x, __fmul_rn(a.x, h));
     v.y = __fadd_rn(v.y, __fmul_rn(a.y, h));
@@ -53,7 +68,6 @@ __device__ __forceinline__ void integrate_body(int64_t i, float4 p, float fx, fl
     v.x = __fadd_rn(v.x, __fmul_rn(fx, h));
     v.y = __fadd_rn(v.y, __fmul_rn(fy, h));
     v.z = __fadd_rn(v.z, __fmul_rn(fz, h));
-    const float4 anew = make_float4(fx, fy, fz, 0.f);
     g.pos_out[i] = p;  // w keeps the mass
     g.vel[i] = v;
     g.acc[i] = anew;

@@ -28,6 +28,7 @@ LIB_PATH = os.path.join(HERE, "libnbody_gb300.so")
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_CAPACITY, ERR_TIMEOUT, ERR_STATE = range(7)
 MODE_PP, MODE_BH = 0, 1
 KEYS_OCTREE, KEYS_MORTON = 0, 1
+INTEGRATOR_CPU, INTEGRATOR_GPU_EULER = 0, 1
 _MODES = {"pp": MODE_PP, "bh": MODE_BH, MODE_PP: MODE_PP, MODE_BH: MODE_BH}
 
 _lib = None
@@ -67,6 +68,7 @@ SIGNATURES = {
     "nbody_bh_counters": (_i, [_vp, _i, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "nbody_set_key_mode": (_i, [_vp, _i]),
     "nbody_diagnostics": (_i, [_vp, ctypes.POINTER(ctypes.c_double)]),
+    "nbody_set_integrator": (_i, [_vp, _i]),
 }
 
 
@@ -287,6 +289,11 @@ class ParticleSolverCUDA:
         v = list(out)
         return {"kinetic": v[0], "potential": v[1], "energy": v[0] + v[1], "momentum": v[2:5],
                 "angular_momentum": v[5:8]}
+
+    def set_integrator(self, kind) -> None:
+        """'cpu' (the reference's CPU order, default) or 'gpu_euler' (its GLSL semi-implicit Euler)."""
+        k = {"cpu": INTEGRATOR_CPU, "gpu_euler": INTEGRATOR_GPU_EULER}.get(kind, kind)
+        self._check(lib().nbody_set_integrator(self._ctx, int(k)), "nbody_set_integrator")
 
     def set_key_mode(self, mode) -> None:
         """'octree' (the reference's FP32 cell descent, default) or 'morton' (morton.glsl quantisation)."""

@@ -111,6 +111,37 @@ def two_discs(n_per_disc_stars: int = 8_388_607, scale_length: float = 200.0, sc
     return _vec4(pos), _vec4(vel), mass
 
 
+def lagrange(world=(5.0, 5.0, 5.0), G: float = 1.0):
+    """The reference's one deterministic initialiser (-i 3,
+    src/ParticleSystemInitializer/ParticleSystemLagrange/ParticleSystemLagrange.cpp:8-50),
+    restated in float32: three bodies of mass 10.5 on an equilateral triangle of
+    side |world| / 10 around the world centre, each moving tangentially at half
+    the speed sqrt(G M / r) for total mass M and distance r to the centre of mass."""
+    f = np.float32
+    w = np.asarray(world, np.float32)
+    mass = f(10.5)
+    side = f(np.sqrt(f(np.dot(w, w)))) / f(10.0)
+    s3 = f(np.sqrt(f(3.0)))
+    c = w / f(2.0)
+    v1 = c + np.array([0.0, side / s3, 0.0], np.float32)
+    v2 = c + np.array([-side / f(2.0), -side / (f(2.0) * s3), 0.0], np.float32)
+    v3 = c + np.array([side / f(2.0), -side / (f(2.0) * s3), 0.0], np.float32)
+    com = (v1 + v2 + v3) / f(3.0)
+    total = mass * f(3)
+    zhat = np.array([0.0, 0.0, 1.0], np.float32)
+    pos = np.zeros((3, 4), np.float32)
+    vel = np.zeros((3, 4), np.float32)
+    for k, vert in enumerate((v1, v2, v3)):
+        d = vert - com
+        r = f(np.sqrt(f(np.dot(d, d))))
+        speed = f(np.sqrt(f(G) * total / r))
+        t = np.cross(d, zhat).astype(np.float32)
+        t = t * (f(1.0) / f(np.sqrt(f(np.dot(t, t)))))
+        pos[k, :3] = vert
+        vel[k, :3] = (t * speed) * f(0.5)
+    return pos, vel, np.full(3, mass, np.float32)
+
+
 def pos_mass(pos4: np.ndarray, mass: np.ndarray) -> np.ndarray:
     """Device layout: (x, y, z, m) per body."""
     out = np.array(pos4, dtype=np.float32, copy=True)
