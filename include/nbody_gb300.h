@@ -107,6 +107,11 @@ int nbody_upload(nbody_ctx *ctx, const float *positions4, const float *velocitie
 int nbody_step(nbody_ctx *ctx, int steps);
 int nbody_download(nbody_ctx *ctx, float *positions4, float *velocities4, float *accelerations4,
                    float *forces4);
+/* Masses of the resident state in the reference layout (masses4[4*i] = m_i,
+ * other components 0), caller's body order. Masses never change during a run;
+ * this is for states made on the device (nbody_init_device). Waits for the
+ * context's stream. */
+int nbody_download_masses(nbody_ctx *ctx, float *masses4);
 /* Waits for the context's stream and returns the device status word
  * (NBODY_OK, or NBODY_ERR_TIMEOUT / NBODY_ERR_CAPACITY raised by a kernel). */
 int nbody_sync(nbody_ctx *ctx);
@@ -141,6 +146,36 @@ int nbody_pp_config(nbody_ctx *ctx, int64_t n, int *bodies_per_thread, int *slic
  * context), out[2..4] linear momentum, out[5..7] angular momentum about the
  * origin. Waits for the context's stream. */
 int nbody_diagnostics(nbody_ctx *ctx, double *out);
+
+/* Seeded initial conditions generated on the GPU straight into the resident
+ * state, in place of nbody_upload (same effect: the next nbody_step starts from
+ * them; body i is caller index i for nbody_download). The reference's
+ * initialisers (src/ParticleSystemInitializer/*, chosen by -i in
+ * src/main.cpp:41-66) seed from the clock or std::random_device; these restate
+ * their shapes with a counter-based generator, so a (kind, seed, params, n)
+ * always gives the same bits. Kinds 1, 2, 4, 5, 6 keep the reference's -i
+ * numbers (include/enums.h:3-11) and take params[0..2] = world dimensions
+ * (default 5, 5, 5, the reference's world); a sphere takes params[3] = velocity
+ * pattern (0 outward, 1 inward, 2 orbit). The galaxy is the reference's first,
+ * fixed-shape branch. Workload kinds (G = 1):
+ *   NBODY_INIT_PLUMMER       params = {a, body mass, truncation / a}      default {100, 1, 20}
+ *   NBODY_INIT_UNIFORM_BALL  params = {radius, mass lo, mass hi}          default {100, 1, 10}
+ *   NBODY_INIT_TWO_DISCS     params = {scale length, scale height, central mass, separation,
+ *                                      relative speed, inclination deg, eps2, star mass}
+ *                                                       default {200, 20, 1e6, 2000, 50, 30, 40, 1}
+ *                            (n even; bodies 0 and n/2 are the central masses)
+ * params may be NULL (all defaults); the first nparams (<= NBODY_INIT_MAX_PARAMS)
+ * replace the defaults. Enqueued on the context's stream. */
+#define NBODY_INIT_CUBE 1
+#define NBODY_INIT_GALAXY 2
+#define NBODY_INIT_SPHERE 4
+#define NBODY_INIT_BALL 5
+#define NBODY_INIT_CUBE_SURFACE 6
+#define NBODY_INIT_PLUMMER 16
+#define NBODY_INIT_UNIFORM_BALL 17
+#define NBODY_INIT_TWO_DISCS 18
+#define NBODY_INIT_MAX_PARAMS 8
+int nbody_init_device(nbody_ctx *ctx, int kind, uint64_t seed, const float *params, int nparams);
 
 /* Selects the integrator (NBODY_INTEGRATOR_*). */
 int nbody_set_integrator(nbody_ctx *ctx, int integrator);

@@ -17,6 +17,7 @@
 
 #include "bh.h"
 #include "diag.h"
+#include "init.h"
 #include "kernels.h"
 #include "nbody_gb300.h"
 #include "sort.h"
@@ -437,6 +438,19 @@ int nbody_download(nbody_ctx *ctx, float *positions4, float *velocities4, float 
     return read_status(ctx);
 }
 
+int nbody_download_masses(nbody_ctx *ctx, float *masses4) {
+    if (!ctx || !masses4) return NBODY_ERR_ARG;
+    if (!ctx->uploaded) return NBODY_ERR_STATE;
+    DeviceGuard dg(ctx->device);
+    const bool bh = ctx->mode == NBODY_MODE_BH;
+    const float4 *pos = bh ? ctx->pos[ctx->bh_pos] : ctx->pos[ctx->cur];
+    const int *ids = (bh && ctx->ids_valid) ? ctx->ids[ctx->bh_va] : nullptr;
+    NB_CK(ctx, nbody::unpack_masses(pos, ids, ctx->stage, ctx->n, ctx->stream, ctx->status));
+    NB_CK(ctx, cudaMemcpyAsync(masses4, ctx->stage, static_cast<size_t>(ctx->n) * sizeof(float4),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+    return read_status(ctx);
+}
+
 int nbody_sync(nbody_ctx *ctx) {
     if (!ctx) return NBODY_ERR_ARG;
     DeviceGuard dg(ctx->device);
@@ -668,6 +682,23 @@ int nbody_diagnostics(nbody_ctx *ctx, double *out) {
     NB_CK(ctx, nbody::diag_momenta(P, V, ctx->diag_phi, n, ctx->diag_mem, out_dev, ctx->stream));
     NB_CK(ctx, cudaMemcpyAsync(out, out_dev, sizeof(double) * 8, cudaMemcpyDeviceToHost, ctx->stream));
     return read_status(ctx);
+}
+
+int nbody_init_device(nbody_ctx *ctx, int kind, uint64_t seed, const float *params, int nparams) {
+    if (!ctx || !nbody::init_kind_valid(kind) || nparams < 0 || nparams > NBODY_INIT_MAX_PARAMS ||
+        (nparams > 0 && !params))
+        return NBODY_ERR_ARG;
+    if (kind == NBODY_INIT_TWO_DISCS && (ctx->n < 2 || ctx->n % 2 != 0)) return NBODY_ERR_ARG;
+    nbody::InitParams prm = nbody::init_defaults(kind);
+    for (int k = 0; k < nparams; ++k) prm.p[k] = params[k];
+    DeviceGuard dg(ctx->device);
+    NB_CK(ctx, nbody::init_state(kind, seed, ctx->n, prm, ctx->pos[0], ctx->vel, ctx->acc, ctx->stream));
+    ctx->cur = 0;
+    ctx->bh_pos = 0;
+    ctx->bh_va = 0;
+    ctx->ids_valid = false;
+    ctx->uploaded = true;
+    return NBODY_OK;
 }
 
 int nbody_set_integrator(nbody_ctx *ctx, int integrator) {

@@ -66,5 +66,8 @@ cudaError_t pp_launch(const PPPlan &plan, const float4 *pos, int64_t n, float ep
 cudaError_t pack_state(const float4 *positions4, const float4 *masses4, float4 *pos_mass, int64_t n,
                        cudaStream_t stream);
 cudaError_t unpack_positions(const float4 *pos_mass, float4 *positions4, int64_t n, cudaStream_t stream);
+// masses4[ids ? ids[i] : i] = (m_i, 0, 0, 0): the reference's vec4 mass layout.
+cudaError_t unpack_masses(const float4 *pos_mass, const int *ids, float4 *masses4, int64_t n, cudaStream_t stream,
+                          int *status);
 
 }  // namespace nbody

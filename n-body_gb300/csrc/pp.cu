@@ -265,6 +265,18 @@ __global__ void unpack_kernel(const float4 *__restrict__ pos_mass, float4 *__res
     positions4[i] = make_float4(p.x, p.y, p.z, 0.f);
 }
 
+__global__ void unpack_masses_kernel(const float4 *__restrict__ pos_mass, const int *__restrict__ ids,
+                                     float4 *__restrict__ masses4, int64_t n, int *status) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t d = ids ? ids[i] : i;
+    if (d < 0 || d >= n) {
+        record_error(status, NBODY_ERR_CAPACITY);
+        return;
+    }
+    masses4[d] = make_float4(pos_mass[i].w, 0.f, 0.f, 0.f);
+}
+
 // ---------------------------------------------------------------- host side
 namespace {
 
@@ -430,6 +442,15 @@ cudaError_t unpack_positions(const float4 *pos_mass, float4 *positions4, int64_t
     const int threads = 256;
     unpack_kernel<<<static_cast<unsigned>((n + threads - 1) / threads), threads, 0, stream>>>(pos_mass,
                                                                                              positions4, n);
+    return cudaGetLastError();
+}
+
+cudaError_t unpack_masses(const float4 *pos_mass, const int *ids, float4 *masses4, int64_t n, cudaStream_t stream,
+                          int *status) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    unpack_masses_kernel<<<static_cast<unsigned>((n + threads - 1) / threads), threads, 0, stream>>>(
+        pos_mass, ids, masses4, n, status);
     return cudaGetLastError();
 }
 

@@ -29,6 +29,13 @@ OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_CAPACITY, ERR_TIMEOUT, ERR_STATE = range(7
 MODE_PP, MODE_BH = 0, 1
 KEYS_OCTREE, KEYS_MORTON = 0, 1
 INTEGRATOR_CPU, INTEGRATOR_GPU_EULER = 0, 1
+# Device-side initial conditions (nbody_init_device); 1..6 are the reference's -i numbers.
+INIT_CUBE, INIT_GALAXY, INIT_SPHERE, INIT_BALL, INIT_CUBE_SURFACE = 1, 2, 4, 5, 6
+INIT_PLUMMER, INIT_UNIFORM_BALL, INIT_TWO_DISCS = 16, 17, 18
+INIT_MAX_PARAMS = 8
+_INIT_KINDS = {"cube": INIT_CUBE, "galaxy": INIT_GALAXY, "sphere": INIT_SPHERE, "ball": INIT_BALL,
+               "cube_surface": INIT_CUBE_SURFACE, "plummer": INIT_PLUMMER, "uniform_ball": INIT_UNIFORM_BALL,
+               "two_discs": INIT_TWO_DISCS}
 _MODES = {"pp": MODE_PP, "bh": MODE_BH, MODE_PP: MODE_PP, MODE_BH: MODE_BH}
 
 _lib = None
@@ -69,6 +76,8 @@ SIGNATURES = {
     "nbody_set_key_mode": (_i, [_vp, _i]),
     "nbody_diagnostics": (_i, [_vp, ctypes.POINTER(ctypes.c_double)]),
     "nbody_set_integrator": (_i, [_vp, _i]),
+    "nbody_init_device": (_i, [_vp, _i, ctypes.c_uint64, ctypes.POINTER(_f), _i]),
+    "nbody_download_masses": (_i, [_vp, _vp]),
 }
 
 
@@ -203,9 +212,13 @@ class ParticleSolverCUDA:
     def step(self, steps: int = 1) -> None:
         self._check(lib().nbody_step(self._ctx, int(steps)), "nbody_step")
 
-    def download(self, system: ParticleSystem) -> None:
+    def download(self, system: ParticleSystem, masses: bool = False) -> None:
+        """Resident state into the host arrays; masses=True also fills the masses
+        (needed after init_device, when the host never held them)."""
         self._check(lib().nbody_download(self._ctx, _ptr(system.positions), _ptr(system.velocities),
                                          _ptr(system.accelerations), _ptr(system.forces)), "nbody_download")
+        if masses:
+            self._check(lib().nbody_download_masses(self._ctx, _ptr(system.masses)), "nbody_download_masses")
 
     def sync(self) -> None:
         self._check(lib().nbody_sync(self._ctx), "nbody_sync")
@@ -289,6 +302,17 @@ class ParticleSolverCUDA:
         v = list(out)
         return {"kinetic": v[0], "potential": v[1], "energy": v[0] + v[1], "momentum": v[2:5],
                 "angular_momentum": v[5:8]}
+
+    def init_device(self, kind, seed: int = 12345, params=None) -> None:
+        """Seeded initial conditions generated on the GPU in place of upload().
+
+        kind: a name of _INIT_KINDS or an INIT_* number; params: up to
+        INIT_MAX_PARAMS floats replacing the kind's defaults in order."""
+        k = _INIT_KINDS.get(kind, kind)
+        vals = [] if params is None else [float(x) for x in params]
+        buf = (_f * max(len(vals), 1))(*vals) if vals else None
+        self._check(lib().nbody_init_device(self._ctx, int(k), ctypes.c_uint64(seed & (2**64 - 1)), buf, len(vals)),
+                    "nbody_init_device")
 
     def set_integrator(self, kind) -> None:
         """'cpu' (the reference's CPU order, default) or 'gpu_euler' (its GLSL semi-implicit Euler)."""

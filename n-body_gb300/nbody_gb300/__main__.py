@@ -10,10 +10,12 @@ registered as two new versions, and replaces its window and render loop
   -v 9   Barnes-Hut on the GPU   (-v 6 semantics: ParticleSolverBHutCPUParallel)
 
 Versions 1-7 are the reference's own CPU and OpenGL solvers and are not part of
-this program. Initialisers: -i 3 (the reference's Lagrange triangle), -i 5
-(uniform ball), -f FILE (the reference's text format, or this library's
-lossless binary format), and --init plummer / discs for the benchmark
-workloads. Defaults follow the reference (-n 100, -t 0.001, -s 0.0935;
+this program. Initialisers (the reference's -i numbers, include/enums.h:3-11):
+-i 1 cube, 2 galaxy, 4 sphere surface, 5 ball, 6 cube surface (generated on
+the GPU from --seed, in the reference's 5 x 5 x 5 world), -i 3 the Lagrange
+triangle, -f FILE (the reference's text format, or this library's lossless
+binary format), and -i plummer / discs for the benchmark workloads (also
+generated on the GPU). Defaults follow the reference (-n 100, -t 0.001, -s 0.0935;
 ArgumentsParser.cpp:6-10). At exit it prints the step count and the mean time
 per step, as the reference's RenderTimer prints its average frame time
 (src/RenderTimer/RenderTimer.cpp:77-94).
@@ -37,7 +39,7 @@ def parse(argv):
     ap = argparse.ArgumentParser(prog="python -m nbody_gb300", allow_abbrev=False)
     ap.add_argument("-v", "-version", dest="version", type=int, default=9)
     ap.add_argument("-n", dest="n", type=int, default=100)
-    ap.add_argument("-i", "-init", dest="init", default="5")
+    ap.add_argument("-i", "-init", dest="init", default="2")  # the reference defaults to the galaxy
     ap.add_argument("-t", "-time-step", dest="dt", type=float, default=0.001)
     ap.add_argument("-s", "-softening", dest="eps2", type=float, default=0.0935)
     ap.add_argument("-f", "-file", dest="file", default=None)
@@ -53,24 +55,28 @@ def parse(argv):
     return ap.parse_args(argv)
 
 
-def initial_system(args) -> ParticleSystem:
+# -i values generated on the device by nbody_init_device.
+DEVICE_INITS = {"1": "cube", "2": "galaxy", "4": "sphere", "5": "ball", "6": "cube_surface",
+                "plummer": "plummer", "discs": "two_discs"}
+
+
+def initial_system(args):
+    """(host system or None, n, device initialiser kind or None)."""
     if args.file:
         with open(args.file, "rb") as f:
             head = f.read(8)
-        return io.load_binary(args.file) if head == io.MAGIC else io.read_text(args.file)
+        system = io.load_binary(args.file) if head == io.MAGIC else io.read_text(args.file)
+        return system, system.n, None
     init = str(args.init)
     if init == "3":
         p, v, m = I.lagrange()
-    elif init in ("5", "ball"):
-        p, v, m = I.uniform_ball(args.n, seed=args.seed)
-    elif init == "plummer":
-        p, v, m = I.plummer(args.n, seed=args.seed)
-    elif init == "discs":
-        p, v, m = I.two_discs(max(1, (args.n - 2) // 2), seed=args.seed)
-    else:
-        sys.stderr.write("Invalid initialization type\n")
-        sys.exit(1)
-    return ParticleSystem(p, v, m)
+        return ParticleSystem(p, v, m), 3, None
+    if init in DEVICE_INITS:
+        kind = DEVICE_INITS[init]
+        n = args.n + (args.n % 2) if kind == "two_discs" else args.n
+        return None, n, kind
+    sys.stderr.write("Invalid initialization type\n")
+    sys.exit(1)
 
 
 def main(argv=None) -> int:
@@ -81,15 +87,20 @@ def main(argv=None) -> int:
     if args.n <= 0:
         sys.stderr.write("Invalid number of particles\n")
         return 1
-    system = initial_system(args)
+    system, n, device_kind = initial_system(args)
     try:
-        solver = ParticleSolverCUDA(args.dt, args.eps2, system.n, mode=VERSIONS[args.version],
+        solver = ParticleSolverCUDA(args.dt, args.eps2, n, mode=VERSIONS[args.version],
                                     theta2=args.theta * args.theta, device=args.device)
         solver.set_integrator(args.integrator)
         if VERSIONS[args.version] == "bh":
             solver.set_key_mode(args.keys)
-        solver.upload(system)
-        print(f"version {args.version} ({VERSIONS[args.version]}), {system.n} bodies, dt {args.dt}, "
+        if device_kind is None:
+            solver.upload(system)
+        else:
+            solver.init_device(device_kind, seed=args.seed)
+            z = np.zeros((n, 4), np.float32)
+            system = ParticleSystem(z, z.copy(), np.zeros(n, np.float32))
+        print(f"version {args.version} ({VERSIONS[args.version]}), {n} bodies, dt {args.dt}, "
               f"eps2 {args.eps2}, {args.steps} steps", flush=True)
         t0 = time.perf_counter()
         done = 0
@@ -105,7 +116,7 @@ def main(argv=None) -> int:
                       flush=True)
         solver.sync()
         secs = time.perf_counter() - t0
-        solver.download(system)
+        solver.download(system, masses=device_kind is not None)
     except NBodyError as e:
         sys.stderr.write(f"{e}\n")
         return 1

@@ -81,7 +81,7 @@ def test_lagrange_initialiser_matches_reference():
 
 @pytest.mark.parametrize("argv,msg", [(["-v", "7"], "Invalid version"), (["-v", "8", "-n", "0"],
                                                                          "Invalid number of particles"),
-                                       (["-v", "8", "-i", "2"], "Invalid initialization type")])
+                                       (["-v", "8", "-i", "8"], "Invalid initialization type")])
 def test_cli_rejects_bad_arguments(argv, msg):
     r = subprocess.run([sys.executable, "-m", "nbody_gb300", *argv], capture_output=True, text=True,
                        cwd=os.path.join(ROOT, "n-body_gb300"))
