@@ -225,6 +225,55 @@ int nbody_profile_read(nbody_ctx *ctx, double *ms, int *launches, int nstages);
 const char *nbody_stage_name(int stage);
 int nbody_stage_count(void);
 
+/* ---------------------------------------------------------------- ensembles
+ * Many independent systems of uneven size stepped together on one GPU (no
+ * counterpart in the reference, which steps one system per process). Each
+ * system keeps the semantics of its solver path: systems with n < crossover
+ * (or added with mode NBODY_MODE_PP) use the direct sum of nbody_create(..,
+ * NBODY_MODE_PP, ..), the others Barnes-Hut (NBODY_MODE_BH) with their own
+ * theta2; every system has its own dt, eps2 and integrator. A system's result
+ * does not depend on the other systems in the ensemble: it is the same alone
+ * and in any mix, bit for bit. Barnes-Hut systems follow the single-system
+ * solver bit for bit; direct-sum systems sum in a different order than the
+ * single-system kernel (which splits j-ranges across CTAs).
+ *
+ * Systems are added and removed between steps; the packed layout is rebuilt at
+ * the next call that needs it (upload, init, step, download), moving the
+ * states of the remaining systems on the device. Every live system must hold
+ * a state (upload or init_device) before a step. nbody_ensemble_step(e, k, g)
+ * runs k steps, in CUDA graphs of g steps each when g > 0 (captured once per
+ * g and buffer parity, then replayed) and the rest one launch sequence at a
+ * time. An ensemble is not re-entrant. */
+typedef struct nbody_ensemble nbody_ensemble;
+int nbody_ensemble_create(nbody_ensemble **out, int device, int64_t crossover);
+int nbody_ensemble_destroy(nbody_ensemble *e);
+const char *nbody_ensemble_last_error(const nbody_ensemble *e);
+int nbody_ensemble_set_stream(nbody_ensemble *e, void *stream);
+/* pp_shape: direct-sum launch shape 0 = 128 threads x 2 bodies, 1 = 256 x 2
+ * (default), 2 = 256 x 4; key_mode: NBODY_KEYS_*. */
+int nbody_ensemble_set_options(nbody_ensemble *e, int pp_shape, int key_mode);
+/* mode: NBODY_MODE_PP, NBODY_MODE_BH, or -1 (by crossover). */
+int nbody_ensemble_add(nbody_ensemble *e, int64_t n, float dt, float eps2, float theta2, int mode, int integrator,
+                       int *system);
+int nbody_ensemble_remove(nbody_ensemble *e, int system);
+int nbody_ensemble_system_info(nbody_ensemble *e, int system, int *mode, int64_t *n);
+/* Host arrays in the reference layout, as nbody_upload; returns once they may be reused. */
+int nbody_ensemble_upload(nbody_ensemble *e, int system, const float *positions4, const float *velocities4,
+                          const float *accelerations4, const float *masses4);
+/* As nbody_init_device, for one system (the same bits as a single-system context). */
+int nbody_ensemble_init_device(nbody_ensemble *e, int system, int kind, uint64_t seed, const float *params,
+                               int nparams);
+int nbody_ensemble_step(nbody_ensemble *e, int steps, int graph_steps);
+/* Waits for the ensemble's stream; any argument may be NULL. */
+int nbody_ensemble_download(nbody_ensemble *e, int system, float *positions4, float *velocities4,
+                            float *accelerations4, float *masses4);
+int nbody_ensemble_sync(nbody_ensemble *e);
+/* Live systems, bodies per group, and kernel launches per step. */
+int nbody_ensemble_counts(nbody_ensemble *e, int *systems, int64_t *pp_bodies, int64_t *bh_bodies,
+                          int *launches_per_step);
+/* Device bytes one system of n bodies takes in an ensemble (for admission). */
+int64_t nbody_ensemble_footprint(int64_t n, int mode);
+
 /* Direct-sum accelerations without any allocation by this library. It has
  * no counterpart in the reference. It is for callers that cannot let a library
  * call cudaMalloc: a frame or control loop that must not stall on an

@@ -50,6 +50,25 @@ __device__ __forceinline__ int level_of(int delta) {
     return l < kMaxLevel ? l : kMaxLevel;
 }
 
+// Several systems packed back to back (an ensemble) are told apart by the
+// per-body system id sv.seg. The radix tree then runs over the composite keys
+// (system id as 32 leading bits, then the 63-bit key, then the index), so
+// delta between bodies of different systems is below 32 and inside a system it
+// is 32 + the key's delta. Nodes with delta < 32 join systems and are no
+// octree cell (level -1); below them each system's subtree is exactly the tree
+// of that system alone. sv.seg == nullptr is the single-system solver.
+__device__ __forceinline__ int level_c(int delta, int base) {
+    return delta < base ? -1 : level_of(delta - base);
+}
+
+__device__ __forceinline__ bool same_key(const uint64_t *__restrict__ k, const SegView &sv, int64_t a, int64_t b) {
+    return k[a] == k[b] && (sv.seg == nullptr || sv.seg[a] == sv.seg[b]);
+}
+
+__device__ __forceinline__ const float *box_of(const SegView &sv, const float *box, int64_t body) {
+    return sv.seg ? sv.boxes + 8 * sv.seg[body] : box;
+}
+
 // ------------------------------------------------------------- bounding box
 // Reference seeds: min = FLT_MAX, max = FLT_MIN (ParallelOctreeCPU.cpp:77-82),
 // strict comparisons. min/max are order-independent, so the result is exact.
@@ -201,12 +220,131 @@ __global__ void morton_kernel(const float4 *__restrict__ pos, int64_t n, const f
     if (vals) vals[i] = static_cast<uint32_t>(i);
 }
 
+// ------------------------------------------- ensemble: per-system boxes
+// Float min / max through unsigned atomics on an order-preserving encoding
+// (exact and order-independent, as the single-system reduction).
+__device__ __forceinline__ unsigned ord_of(float f) {
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float float_of(unsigned o) {
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+
+// One CTA per chunk of one system (chunk = {system, first, end, chunks of the
+// system}). Accumulators start at the reference's seeds (min FLT_MAX, max
+// FLT_MIN); the system's last chunk writes the box and re-seeds them.
+__global__ void __launch_bounds__(256) bbox_seg_kernel(const float4 *__restrict__ pos,
+                                                       const int4 *__restrict__ chunks,
+                                                       unsigned *__restrict__ acc, float *__restrict__ boxes) {
+    const int4 c = chunks[blockIdx.x];
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+    float mx[3] = {FLT_MIN, FLT_MIN, FLT_MIN};
+    for (int i = c.y + threadIdx.x; i < c.z; i += blockDim.x) {
+        const float4 p = pos[i];
+        if (p.x < mn[0]) mn[0] = p.x;
+        if (p.y < mn[1]) mn[1] = p.y;
+        if (p.z < mn[2]) mn[2] = p.z;
+        if (p.x > mx[0]) mx[0] = p.x;
+        if (p.y > mx[1]) mx[1] = p.y;
+        if (p.z > mx[2]) mx[2] = p.z;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float o1 = __shfl_down_sync(0xffffffffu, mn[a], off);
+            const float o2 = __shfl_down_sync(0xffffffffu, mx[a], off);
+            if (o1 < mn[a]) mn[a] = o1;
+            if (o2 > mx[a]) mx[a] = o2;
+        }
+    }
+    __shared__ float wm[8][6];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int a = 0; a < 3; ++a) {
+            wm[warp][a] = mn[a];
+            wm[warp][3 + a] = mx[a];
+        }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w)
+        for (int a = 0; a < 3; ++a) {
+            if (wm[w][a] < wm[0][a]) wm[0][a] = wm[w][a];
+            if (wm[w][3 + a] > wm[0][3 + a]) wm[0][3 + a] = wm[w][3 + a];
+        }
+    unsigned *A = acc + 8 * c.x;
+    for (int a = 0; a < 3; ++a) {
+        atomicMin(&A[a], ord_of(wm[0][a]));
+        atomicMax(&A[3 + a], ord_of(wm[0][3 + a]));
+    }
+    __threadfence();
+    if (atomicAdd(&A[6], 1u) != static_cast<unsigned>(c.w - 1)) return;
+    __threadfence();
+    float *B = boxes + 8 * c.x;
+    for (int a = 0; a < 6; ++a) B[a] = float_of(atomicAdd(&A[a], 0u));
+    for (int a = 0; a < 3; ++a) {
+        A[a] = ord_of(FLT_MAX);
+        A[3 + a] = ord_of(FLT_MIN);
+    }
+    A[6] = 0u;
+}
+
+__global__ void seed_box_acc_kernel(unsigned *__restrict__ acc, int systems) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= systems) return;
+    for (int a = 0; a < 3; ++a) {
+        acc[8 * s + a] = ord_of(FLT_MAX);
+        acc[8 * s + 3 + a] = ord_of(FLT_MIN);
+    }
+    acc[8 * s + 6] = 0u;
+    acc[8 * s + 7] = 0u;
+}
+
+// Keys over each body's own system box; the unsorted keys are kept for the
+// gather (the segment passes of the sort overwrite the key array).
+template <int MODE>
+__global__ void keys_seg_kernel(const float4 *__restrict__ pos, int64_t n, const int *__restrict__ seg,
+                                const float *__restrict__ boxes, uint64_t *__restrict__ keys,
+                                uint64_t *__restrict__ keys_orig, uint32_t *__restrict__ vals) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos[i];
+    const float *box = boxes + 8 * seg[i];
+    uint64_t key;
+    if (MODE == NBODY_KEYS_MORTON) {
+        const uint64_t qx = quantize21(p.x, box[0], box[3]);
+        const uint64_t qy = quantize21(p.y, box[1], box[4]);
+        const uint64_t qz = quantize21(p.z, box[2], box[5]);
+        key = (expand21(qx) << 2) | (expand21(qy) << 1) | expand21(qz);
+    } else {
+        key = octree_key(p.x, p.y, p.z, box);
+    }
+    keys[i] = key;
+    keys_orig[i] = key;
+    vals[i] = static_cast<uint32_t>(i);
+}
+
+// Sort key of the segment passes: the system of the body now at slot j.
+__global__ void seg_keys_kernel(const uint32_t *__restrict__ vals, int64_t n, const int *__restrict__ seg,
+                                uint64_t *__restrict__ out, int *status) {
+    const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t v = vals[j];
+    if (v >= static_cast<uint64_t>(n)) {
+        record_error(status, NBODY_ERR_CAPACITY);
+        v = 0;
+    }
+    out[j] = static_cast<uint64_t>(seg[v]);
+}
+
 // ------------------------------------------------------------------ gather
 __global__ void gather_kernel(const uint32_t *__restrict__ perm, int64_t n, const float4 *__restrict__ pos_in,
                               const float4 *__restrict__ vel_in, const float4 *__restrict__ acc_in,
                               const int *__restrict__ id_in, float4 *__restrict__ pos_out,
                               float4 *__restrict__ vel_out, float4 *__restrict__ acc_out,
-                              int *__restrict__ id_out, int *status) {
+                              int *__restrict__ id_out, int *status, const uint64_t *__restrict__ key_in,
+                              uint64_t *__restrict__ key_out) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t j = perm[i];
@@ -218,34 +356,43 @@ __global__ void gather_kernel(const uint32_t *__restrict__ perm, int64_t n, cons
     if (vel_out) vel_out[i] = vel_in[j];
     if (acc_out) acc_out[i] = acc_in[j];
     if (id_out) id_out[i] = id_in ? id_in[j] : static_cast<int>(j);
+    if (key_out) key_out[i] = key_in[j];
 }
 
 // ------------------------------------------------------ binary radix tree
-__device__ __forceinline__ int delta_at(const uint64_t *__restrict__ k, int64_t n, int64_t i, int64_t j) {
+__device__ __forceinline__ int delta_at(const uint64_t *__restrict__ k, const int *__restrict__ seg, int64_t n,
+                                        int64_t i, int64_t j) {
     if (j < 0 || j >= n) return -1;
+    int base = 0;
+    if (seg) {
+        const int si = seg[i], sj = seg[j];
+        if (si != sj) return __clz(si ^ sj);
+        base = 32;
+    }
     const uint64_t a = k[i], b = k[j];
-    if (a != b) return __clzll(static_cast<long long>(a ^ b)) - 1;  // bit 63 is always 0
-    return 63 + __clz(static_cast<int>(i ^ j));                         // equal keys: break ties by index
+    if (a != b) return base + __clzll(static_cast<long long>(a ^ b)) - 1;  // bit 63 is always 0
+    return base + 63 + __clz(static_cast<int>(i ^ j));                        // equal keys: break ties by index
 }
 
-__global__ void radix_tree_kernel(const uint64_t *__restrict__ k, int64_t n, BinaryTree t) {
+__global__ void radix_tree_kernel(const uint64_t *__restrict__ k, int64_t n, BinaryTree t, SegView sv) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
-    const int dl = delta_at(k, n, i, i - 1), dr = delta_at(k, n, i, i + 1);
+    const int *seg = sv.seg;
+    const int dl = delta_at(k, seg, n, i, i - 1), dr = delta_at(k, seg, n, i, i + 1);
     const int d = dr > dl ? 1 : -1;
     const int dmin = d > 0 ? dl : dr;
     int64_t lmax = 2;
-    while (delta_at(k, n, i, i + lmax * d) > dmin) lmax *= 2;
+    while (delta_at(k, seg, n, i, i + lmax * d) > dmin) lmax *= 2;
     int64_t l = 0;
     for (int64_t s = lmax / 2; s >= 1; s /= 2)
-        if (delta_at(k, n, i, i + (l + s) * d) > dmin) l += s;
+        if (delta_at(k, seg, n, i, i + (l + s) * d) > dmin) l += s;
     const int64_t j = i + l * d;
-    const int dnode = delta_at(k, n, i, j);
+    const int dnode = delta_at(k, seg, n, i, j);
     int64_t s = 0;
     int64_t step = l;
     do {
         step = (step + 1) >> 1;
-        if (delta_at(k, n, i, i + (s + step) * d) > dnode) s += step;
+        if (delta_at(k, seg, n, i, i + (s + step) * d) > dnode) s += step;
     } while (step > 1);
     const int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
     const int64_t lo = i < j ? i : j, hi = i < j ? j : i;
@@ -262,21 +409,21 @@ __global__ void radix_tree_kernel(const uint64_t *__restrict__ k, int64_t n, Bin
 }
 
 // Cell tops: radix-tree nodes whose octree level exceeds their parent's.
-__global__ void mark_cells_kernel(int64_t n, BinaryTree t, uint32_t *__restrict__ mask) {
+__global__ void mark_cells_kernel(int64_t n, BinaryTree t, uint32_t *__restrict__ mask, int base) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
-    const int L = level_of(t.delta[i]);
-    const int Lp = i == 0 ? -1 : level_of(t.delta[t.iparent[i]]);
+    const int L = level_c(t.delta[i], base);
+    const int Lp = i == 0 ? -1 : level_c(t.delta[t.iparent[i]], base);
     const bool top = L > Lp;
     t.top[i] = top ? 1 : 0;
     if (top) atomicOr(&mask[t.lo[i]], 1u << L);
 }
 
 __global__ void count_nodes_kernel(const uint64_t *__restrict__ k, int64_t n, const uint32_t *__restrict__ mask,
-                                   uint32_t *__restrict__ cnt) {
+                                   uint32_t *__restrict__ cnt, SegView sv) {
     const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (b >= n) return;
-    const bool lone = !((b > 0 && k[b] == k[b - 1]) || (b + 1 < n && k[b] == k[b + 1]));
+    const bool lone = !((b > 0 && same_key(k, sv, b, b - 1)) || (b + 1 < n && same_key(k, sv, b, b + 1)));
     cnt[b] = __popc(mask[b]) + (lone ? 1u : 0u);
 }
 
@@ -303,8 +450,8 @@ __device__ __forceinline__ float cell_side2(uint64_t key, int L, const float *__
 
 // Record index of the cell whose top radix-tree node is p.
 __device__ __forceinline__ int record_of(const BinaryTree &t, const uint32_t *__restrict__ mask,
-                                         const uint32_t *__restrict__ P, int p) {
-    const int L = level_of(t.delta[p]);
+                                         const uint32_t *__restrict__ P, int p, int base) {
+    const int L = level_c(t.delta[p], base);
     const int lo = t.lo[p];
     return static_cast<int>(P[lo] + __popc(mask[lo] & ((1u << L) - 1u)));
 }
@@ -312,45 +459,49 @@ __device__ __forceinline__ int record_of(const BinaryTree &t, const uint32_t *__
 // Octree parent of a record: the nearest radix-tree ancestor that is a cell
 // top (the nodes in between split the same cell; at most 6 of them).
 __device__ __forceinline__ int octree_parent(const BinaryTree &t, const uint32_t *__restrict__ mask,
-                                             const uint32_t *__restrict__ P, int p) {
-    for (int guard = 0; p >= 0 && !t.top[p] && guard < 96; ++guard) p = t.iparent[p];
-    return (p >= 0 && t.top[p]) ? record_of(t, mask, P, p) : -1;
+                                             const uint32_t *__restrict__ P, int p, int base) {
+    // At most 6 nodes per octree level inside a system, and at most 32 joining
+    // nodes (strictly decreasing delta < 32) above a system's subtree.
+    for (int guard = 0; p >= 0 && !t.top[p] && guard < 160; ++guard) p = t.iparent[p];
+    return (p >= 0 && t.top[p]) ? record_of(t, mask, P, p, base) : -1;
 }
 
 __global__ void emit_cells_kernel(const uint64_t *__restrict__ k, int64_t n, BinaryTree t,
                                   const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
-                                  const float *__restrict__ box, BHNode *__restrict__ nodes, Records r) {
+                                  const float *__restrict__ box, BHNode *__restrict__ nodes, Records r, SegView sv) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     if (!t.top[i]) return;
-    const int L = level_of(t.delta[i]);
+    const int base = sv.seg ? 32 : 0;
+    const int L = level_c(t.delta[i], base);
     const int lo = t.lo[i], hi = t.hi[i];
-    const int idx = record_of(t, mask, P, static_cast<int>(i));
+    const int idx = record_of(t, mask, P, static_cast<int>(i), base);
     int4 meta;
     if (L < kMaxLevel) {
-        meta = make_int4(__float_as_int(cell_side2(k[lo], L, box)), static_cast<int>(P[hi + 1]), lo, 0);
+        meta = make_int4(__float_as_int(cell_side2(k[lo], L, box_of(sv, box, lo))), static_cast<int>(P[hi + 1]), lo,
+                         0);
     } else {  // bucket of bodies with identical keys: a leaf
         meta = make_int4(__float_as_int(-1.f), static_cast<int>(P[hi + 1]), lo, hi - lo + 1);
     }
     nodes[idx].meta = meta;
     r.level[idx] = L;
-    const int par = i == 0 ? -1 : octree_parent(t, mask, P, t.iparent[i]);
+    const int par = i == 0 ? -1 : octree_parent(t, mask, P, t.iparent[i], base);
     r.parent[idx] = par;
     if (par >= 0) atomicAdd(&r.nchild[par], 1);
 }
 
 __global__ void emit_leaves_kernel(const uint64_t *__restrict__ k, int64_t n, const float4 *__restrict__ pos,
                                    BinaryTree t, const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
-                                   BHNode *__restrict__ nodes, Records r) {
+                                   BHNode *__restrict__ nodes, Records r, SegView sv) {
     const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (b >= n) return;
-    const bool lone = !((b > 0 && k[b] == k[b - 1]) || (b + 1 < n && k[b] == k[b + 1]));
+    const bool lone = !((b > 0 && same_key(k, sv, b, b - 1)) || (b + 1 < n && same_key(k, sv, b, b + 1)));
     if (!lone) return;
     const int idx = static_cast<int>(P[b] + __popc(mask[b]));
     nodes[idx].cm = pos[b];
     nodes[idx].meta = make_int4(__float_as_int(-1.f), static_cast<int>(P[b + 1]), static_cast<int>(b), 1);
     r.level[idx] = kMaxLevel + 1;  // a lone body
-    const int par = n < 2 ? -1 : octree_parent(t, mask, P, t.lparent[b]);
+    const int par = n < 2 ? -1 : octree_parent(t, mask, P, t.lparent[b], sv.seg ? 32 : 0);
     r.parent[idx] = par;
     if (par >= 0) atomicAdd(&r.nchild[par], 1);
 }
@@ -383,11 +534,12 @@ __device__ __forceinline__ float4 round_trips(float4 c, int times) {
 
 __global__ void upsweep_kernel(const uint64_t *__restrict__ k, int64_t n, const float4 *__restrict__ pos,
                                const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
-                               BHNode *__restrict__ nodes, Records r, int father_depth, int *status) {
+                               BHNode *__restrict__ nodes, Records r, int father_depth, int *status, SegView sv) {
     const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (b >= n) return;
-    const bool left_eq = b > 0 && k[b] == k[b - 1];
-    const bool right_eq = b + 1 < n && k[b] == k[b + 1];
+    if (sv.seg) father_depth = sv.fdepth[sv.seg[b]];
+    const bool left_eq = b > 0 && same_key(k, sv, b, b - 1);
+    const bool right_eq = b + 1 < n && same_key(k, sv, b, b + 1);
     int rec;
     if (!left_eq && !right_eq) {
         rec = static_cast<int>(P[b] + __popc(mask[b]));  // lone body: already written
@@ -395,7 +547,7 @@ __global__ void upsweep_kernel(const uint64_t *__restrict__ k, int64_t n, const 
         // first body of a bucket: its record is the level-21 cell starting here
         rec = static_cast<int>(P[b] + __popc(mask[b] & ((1u << kMaxLevel) - 1u)));
         float cx = 0.f, cy = 0.f, cz = 0.f, m = 0.f;
-        for (int64_t q = b; q < n && k[q] == k[b]; ++q) {
+        for (int64_t q = b; q < n && same_key(k, sv, q, b); ++q) {
             const float4 o = pos[q];
             if (!(o.w > 0.f)) continue;
             cx = __fadd_rn(cx, __fmul_rn(o.x, o.w));
@@ -629,7 +781,11 @@ __device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, 
 
 // POT also accumulates the potential -sum m / sqrt(d^2 + eps^2) over the same
 // accepted records (for the energy diagnostic) into phi_out[ids[b]].
-template <bool COUNT, bool POT>
+// SEG: an ensemble of systems; warp w serves work[w] = {system, first body
+// of the warp, first body of the system, end of the system}, walks only the
+// system's records [P[first], P[end]) and takes dt, eps2, theta2 and the
+// integrator from params[system] = {dt, eps2, theta2, euler}.
+template <bool COUNT, bool POT, bool SEG>
 __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict__ nodes,
                                                         const uint32_t *__restrict__ node_total,
                                                         const float4 *__restrict__ pos, int64_t n, float eps2,
@@ -637,21 +793,42 @@ __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict
                                                         float4 *__restrict__ vel, float4 *__restrict__ acc,
                                                         float4 *__restrict__ force_out, const int *__restrict__ ids,
                                                         unsigned long long *__restrict__ counters,
-                                                        float *__restrict__ phi_out, int euler) {
+                                                        float *__restrict__ phi_out, int euler,
+                                                        const int4 *__restrict__ work, int nwork,
+                                                        const float4 *__restrict__ params,
+                                                        const uint32_t *__restrict__ P) {
     unsigned long long n_pairs = 0, n_visits = 0;
     float phiA = 0.f, phiB = 0.f;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const int64_t bA = warp * 64 + lane, bB = bA + 32;
-    const bool vA = bA < n, vB = bB < n;
-    const int m_nodes = static_cast<int>(*node_total);
+    int64_t base, end;
+    int i, m_nodes;
+    if (SEG) {
+        if (warp >= nwork) return;  // whole warps
+        const int4 ww = work[warp];
+        const float4 prm = params[ww.x];
+        dt = prm.x;
+        eps2 = prm.y;
+        theta2 = prm.z;
+        euler = prm.w != 0.f ? 1 : 0;
+        base = ww.y;
+        end = ww.w;
+        i = static_cast<int>(P[ww.z]);
+        m_nodes = static_cast<int>(P[ww.w]);
+    } else {
+        base = warp * 64;
+        end = n;
+        i = 0;
+        m_nodes = static_cast<int>(*node_total);
+    }
+    const int64_t bA = base + lane, bB = bA + 32;
+    const bool vA = bA < end, vB = bB < end;
     const float4 meA = vA ? pos[bA] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 meB = vB ? pos[bB] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float2 nx = make_float2(-meA.x, -meB.x), ny = make_float2(-meA.y, -meB.y), nz = make_float2(-meA.z, -meB.z);
     const float2 th = make_float2(theta2, theta2);
-    int skipA = vA ? 0 : m_nodes, skipB = vB ? 0 : m_nodes;
+    int skipA = vA ? i : m_nodes, skipB = vB ? i : m_nodes;
     float fAx = 0.f, fAy = 0.f, fAz = 0.f, fBx = 0.f, fBy = 0.f, fBz = 0.f;
-    int i = 0;
     while (i < m_nodes) {
         const float4 cm = __ldg(&nodes[i].cm);
         const int4 meta = __ldg(&nodes[i].meta);
@@ -848,6 +1025,8 @@ int father_depth(int64_t n) {
 
 }  // namespace
 
+int bh_father_depth(int64_t n) { return father_depth(n); }
+
 // ------------------------------------------------------------------- host
 size_t bh_workspace_bytes(int64_t n) {
     BHWorkspace w;
@@ -934,22 +1113,22 @@ cudaError_t bh_gather(int64_t n, const BHWorkspace &w, const float4 *pos_in, con
                       int *id_out, cudaStream_t st, int *status, StageTimer *timer) {
     if (timer) timer->begin(kStageGather, st);
     gather_kernel<<<grid_for(n, 256), 256, 0, st>>>(w.vals[0], n, pos_in, vel_in, acc_in, id_in, pos_out, vel_out,
-                                                    acc_out, id_out, status);
+                                                    acc_out, id_out, status, nullptr, nullptr);
     if (timer) timer->end(kStageGather, st);
     return cudaGetLastError();
 }
 
 cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaStream_t st, int *status,
-                     StageTimer *timer) {
+                     StageTimer *timer, const SegView &sv) {
     if (timer) timer->begin(kStageBuild, st);
     const uint64_t *k = w.keys[0];
     cudaError_t e = cudaMemsetAsync(w.mask, 0, sizeof(uint32_t) * static_cast<size_t>(n), st);
     if (e != cudaSuccess) return e;
     if (n >= 2) {
-        radix_tree_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(k, n, w.tree);
-        mark_cells_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(n, w.tree, w.mask);
+        radix_tree_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(k, n, w.tree, sv);
+        mark_cells_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(n, w.tree, w.mask, sv.seg ? 32 : 0);
     }
-    count_nodes_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, w.mask, w.cnt);
+    count_nodes_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, w.mask, w.cnt, sv);
     const int tiles = static_cast<int>((n + kScanTile - 1) / kScanTile);
     scan_tiles_kernel<<<tiles, kScanThreads, 0, st>>>(w.cnt, n, w.P, w.scan_sums);
     scan_sums_kernel<<<1, 1024, 0, st>>>(w.scan_sums, tiles, w.P + n);
@@ -959,12 +1138,13 @@ cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaSt
     if (e == cudaSuccess) e = cudaMemsetAsync(w.rec.arrive, 0, sizeof(unsigned) * nrec, st);
     if (e != cudaSuccess) return e;
     if (n >= 2)
-        emit_cells_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(k, n, w.tree, w.mask, w.P, w.box, w.nodes, w.rec);
-    emit_leaves_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.tree, w.mask, w.P, w.nodes, w.rec);
+        emit_cells_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(k, n, w.tree, w.mask, w.P, w.box, w.nodes, w.rec,
+                                                                sv);
+    emit_leaves_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.tree, w.mask, w.P, w.nodes, w.rec, sv);
     if (timer) timer->end(kStageBuild, st);
     if (timer) timer->begin(kStageUpsweep, st);
     upsweep_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.mask, w.P, w.nodes, w.rec,
-                                                     father_depth(n), status);
+                                                     father_depth(n), status, sv);
     if (timer) timer->end(kStageUpsweep, st);
     return cudaGetLastError();
 }
@@ -978,13 +1158,13 @@ cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &
         const int64_t warps = (n + 63) / 64;
         const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
         if (w.counters)
-            traverse2_kernel<true, false><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
-                                                                  pos_out, vel, acc, force_out, ids, w.counters,
-                                                                  nullptr, euler);
+            traverse2_kernel<true, false, false><<<blocks, 256, 0, st>>>(
+                w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, w.counters,
+                nullptr, euler, nullptr, 0, nullptr, nullptr);
         else
-            traverse2_kernel<false, false><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
-                                                                   pos_out, vel, acc, force_out, ids, nullptr,
-                                                                   nullptr, euler);
+            traverse2_kernel<false, false, false><<<blocks, 256, 0, st>>>(
+                w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, nullptr,
+                nullptr, euler, nullptr, 0, nullptr, nullptr);
     } else if (w.counters)
         traverse_kernel<true><<<grid_for(n, 256), 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
                                                                 pos_out, vel, acc, force_out, ids, w.counters, euler);
@@ -999,8 +1179,75 @@ cudaError_t bh_potential(const float4 *pos_sorted, int64_t n, const BHWorkspace 
                          float *phi_out, const int *ids, cudaStream_t st) {
     const int64_t warps = (n + 63) / 64;
     const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
-    traverse2_kernel<false, true><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, 0.f, nullptr,
-                                                          nullptr, nullptr, nullptr, ids, nullptr, phi_out, 0);
+    traverse2_kernel<false, true, false><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, 0.f,
+                                                                 nullptr, nullptr, nullptr, nullptr, ids, nullptr,
+                                                                 phi_out, 0, nullptr, 0, nullptr, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t bh_seed_boxes(const BHEnsembleTables &e, cudaStream_t st) {
+    if (e.systems <= 0) return cudaSuccess;
+    seed_box_acc_kernel<<<grid_for(e.systems, 256), 256, 0, st>>>(e.box_acc, e.systems);
+    return cudaGetLastError();
+}
+
+cudaError_t bh_ensemble_step(int64_t n, BHWorkspace &w, const BHEnsembleTables &e, int key_mode, float4 *P,
+                             float4 *Po, float4 *V, float4 *Vo, float4 *A, float4 *Ao, const int *I, int *Io,
+                             cudaStream_t st, int *status, StageTimer *tm) {
+    if (n <= 0 || e.systems <= 0) return cudaSuccess;
+    cudaError_t err;
+    if (tm) tm->begin(kStageBBox, st);
+    bbox_seg_kernel<<<e.nchunks, 256, 0, st>>>(P, e.chunks, e.box_acc, e.boxes);
+    if (tm) tm->end(kStageBBox, st);
+    if (tm) tm->begin(kStageMorton, st);
+    if (key_mode == NBODY_KEYS_MORTON)
+        keys_seg_kernel<NBODY_KEYS_MORTON><<<grid_for(n, 256), 256, 0, st>>>(P, n, e.seg, e.boxes, w.keys[0],
+                                                                              e.keys_orig, w.vals[0]);
+    else
+        keys_seg_kernel<NBODY_KEYS_OCTREE><<<grid_for(n, 256), 256, 0, st>>>(P, n, e.seg, e.boxes, w.keys[0],
+                                                                              e.keys_orig, w.vals[0]);
+    if (tm) tm->end(kStageMorton, st);
+    if (tm) tm->begin(kStageSort, st);
+    // Stable by key over all systems, then stable by system: within each
+    // system the order is the single-system sort's.
+    int alt = 0;
+    err = sort_pairs(w.keys[0], w.vals[0], w.keys[1], w.vals[1], n, w.sort_scratch, st, status, &alt, 8);
+    if (err != cudaSuccess) return err;
+    uint64_t *k0 = alt ? w.keys[1] : w.keys[0], *k1 = alt ? w.keys[0] : w.keys[1];
+    uint32_t *v0 = alt ? w.vals[1] : w.vals[0], *v1 = alt ? w.vals[0] : w.vals[1];
+    if (e.systems > 1) {
+        seg_keys_kernel<<<grid_for(n, 256), 256, 0, st>>>(v0, n, e.seg, k0, status);
+        err = sort_pairs(k0, v0, k1, v1, n, w.sort_scratch, st, status, &alt, e.seg_passes);
+        if (err != cudaSuccess) return err;
+        if (alt) {
+            uint32_t *tv = v0; v0 = v1; v1 = tv;
+        }
+    }
+    if (tm) tm->end(kStageSort, st);
+    if (tm) tm->begin(kStageGather, st);
+    // Sorted keys into keys[0] (the build reads them there), permutation in vals[0].
+    uint64_t *ksorted = w.keys[0];
+    gather_kernel<<<grid_for(n, 256), 256, 0, st>>>(v0, n, P, V, A, I, Po, Vo, Ao, Io, status, e.keys_orig, ksorted);
+    if (tm) tm->end(kStageGather, st);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    SegView sv;
+    sv.seg = e.seg;
+    sv.boxes = e.boxes;
+    sv.fdepth = e.fdepth;
+    err = bh_build(Po, n, w, st, status, tm, sv);
+    if (err != cudaSuccess) return err;
+    if (tm) tm->begin(kStageTraverse, st);
+    const unsigned blocks = static_cast<unsigned>((static_cast<int64_t>(e.nwarps) * 32 + 255) / 256);
+    if (w.counters)
+        traverse2_kernel<true, false, true><<<blocks, 256, 0, st>>>(w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo,
+                                                                    Ao, nullptr, nullptr, w.counters, nullptr, 0,
+                                                                    e.warps, e.nwarps, e.params, w.P);
+    else
+        traverse2_kernel<false, false, true><<<blocks, 256, 0, st>>>(w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo,
+                                                                     Ao, nullptr, nullptr, nullptr, nullptr, 0,
+                                                                     e.warps, e.nwarps, e.params, w.P);
+    if (tm) tm->end(kStageTraverse, st);
     return cudaGetLastError();
 }
 

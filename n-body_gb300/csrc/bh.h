@@ -34,6 +34,15 @@ struct Records {
     unsigned *arrive;
 };
 
+// Systems packed back to back (an ensemble): seg[b] = system of body b,
+// boxes = 8 floats per system (min xyz, max xyz, 2 unused), fdepth = the
+// reference's fixed top-level depth per system. seg == nullptr: one system.
+struct SegView {
+    const int *seg = nullptr;
+    const float *boxes = nullptr;
+    const int *fdepth = nullptr;
+};
+
 struct BHWorkspace {
     int64_t n = 0;
     uint64_t *keys[2] = {nullptr, nullptr};
@@ -71,7 +80,7 @@ cudaError_t bh_gather(int64_t n, const BHWorkspace &w, const float4 *pos_in, con
                       const float4 *acc_in, const int *id_in, float4 *pos_out, float4 *vel_out, float4 *acc_out,
                       int *id_out, cudaStream_t st, int *status, StageTimer *timer);
 cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaStream_t st, int *status,
-                     StageTimer *timer);
+                     StageTimer *timer, const SegView &sv = SegView{});
 // Forces for every sorted body; with pos_out set, also the reference
 // integrator (pos_out must not alias pos_sorted). force_out, if set, receives
 // the acceleration at index ids[b] (or b when ids is null).
@@ -83,6 +92,33 @@ cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &
 // accepted records as the forces, into phi_out[ids[b]] (or phi_out[b]).
 cudaError_t bh_potential(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,
                          float *phi_out, const int *ids, cudaStream_t st);
+// Tables of an ensemble of Barnes-Hut systems packed back to back in one
+// workspace (all body indices are global positions in the packed arrays).
+struct BHEnsembleTables {
+    int systems = 0;
+    int *seg = nullptr;             // per body: its system
+    int4 *chunks = nullptr;         // bounding-box chunks: system, first, end, chunks of the system
+    int nchunks = 0;
+    unsigned *box_acc = nullptr;    // per system, 8: encoded min xyz, max xyz, arrivals, unused
+    float *boxes = nullptr;         // per system, 8: min xyz, max xyz, unused
+    int *fdepth = nullptr;          // per system: the reference's fixed top-level depth
+    int4 *warps = nullptr;          // traversal work: system, first body, system first, system end
+    int nwarps = 0;
+    float4 *params = nullptr;       // per system: dt, eps2, theta2, euler (0 / 1)
+    uint64_t *keys_orig = nullptr;  // per body: unsorted key
+    int seg_passes = 1;             // 8-bit digits of the system id
+};
+
+// Host helper: the reference's fixed top-level depth for n bodies.
+int bh_father_depth(int64_t n);
+// Seeds the per-system box accumulators (once after the tables are made).
+cudaError_t bh_seed_boxes(const BHEnsembleTables &e, cudaStream_t st);
+// One step of every system: positions P (updated in place), velocity and
+// acceleration V, A -> Vo, Ao, ids I -> Io (I null: identity), Po scratch.
+cudaError_t bh_ensemble_step(int64_t n, BHWorkspace &w, const BHEnsembleTables &e, int key_mode, float4 *P,
+                             float4 *Po, float4 *V, float4 *Vo, float4 *A, float4 *Ao, const int *I, int *Io,
+                             cudaStream_t st, int *status, StageTimer *tm);
+
 cudaError_t bh_unpermute(const int *ids, int64_t n, const float4 *in, float4 *out, bool zero_w, cudaStream_t st,
                          int *status);
 

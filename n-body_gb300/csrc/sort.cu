@@ -17,6 +17,8 @@
 // and writes it out.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "common.cuh"
 #include "sort.h"
 
@@ -40,8 +42,9 @@ __device__ __forceinline__ uint32_t digit_of(uint64_t k, int pass) {
     return static_cast<uint32_t>(k >> (pass * kRadixBits)) & (kBins - 1);
 }
 
-// Global histograms of all 8 digits in one read of the keys.
+// Global histograms of the first `passes` digits in one read of the keys.
 __global__ void __launch_bounds__(kSortThreads) histogram_kernel(const uint64_t *__restrict__ keys, int64_t n,
+                                                                 int passes,
                                                                  uint32_t *__restrict__ hist /* [kPasses][kBins] */) {
     __shared__ uint32_t h[kPasses][kBins];
     for (int i = threadIdx.x; i < kPasses * kBins; i += blockDim.x) (&h[0][0])[i] = 0;
@@ -50,10 +53,11 @@ __global__ void __launch_bounds__(kSortThreads) histogram_kernel(const uint64_t 
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
         const uint64_t k = keys[i];
 #pragma unroll
-        for (int p = 0; p < kPasses; ++p) atomicAdd(&h[p][digit_of(k, p)], 1u);
+        for (int p = 0; p < kPasses; ++p)
+            if (p < passes) atomicAdd(&h[p][digit_of(k, p)], 1u);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < kPasses * kBins; i += blockDim.x) {
+    for (int i = threadIdx.x; i < passes * kBins; i += blockDim.x) {
         const uint32_t v = (&h[0][0])[i];
         if (v) atomicAdd(&hist[i], v);
     }
@@ -234,33 +238,49 @@ size_t sort_scratch_bytes(int64_t n) {
     return (b + 255) & ~static_cast<size_t>(255);
 }
 
+cudaError_t sort_prepare(int device) {
+    static std::mutex mu;
+    static bool done[64] = {};
+    std::lock_guard<std::mutex> lk(mu);
+    if (device >= 0 && device < 64 && done[device]) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(onesweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(sizeof(SortSmem)));
+    if (e == cudaSuccess && device >= 0 && device < 64) done[device] = true;
+    return e;
+}
+
 cudaError_t sort_pairs(uint64_t *keys, uint32_t *vals, uint64_t *keys_alt, uint32_t *vals_alt, int64_t n,
-                       void *scratch, cudaStream_t stream, int *status, int *result_in_alt) {
+                       void *scratch, cudaStream_t stream, int *status, int *result_in_alt, int passes) {
     *result_in_alt = 0;
-    if (n <= 1) return cudaSuccess;
+    if (n <= 1 || passes <= 0) return cudaSuccess;
+    if (passes > kPasses) return cudaErrorInvalidValue;
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e == cudaSuccess) e = sort_prepare(device);
+    if (e != cudaSuccess) return e;
     const int64_t tiles = (n + kTile - 1) / kTile;
     uint32_t *hist = static_cast<uint32_t *>(scratch);
     uint32_t *counters = hist + kPasses * kBins;
     uint32_t *desc = counters + 64;
-    cudaError_t e = cudaMemsetAsync(scratch, 0, sort_scratch_bytes(n), stream);
+    // Only what this sort uses must start at zero: histograms, tile counters and
+    // the look-back descriptors of `passes` passes.
+    const size_t used = sizeof(uint32_t) * (kPasses * kBins + 64 + static_cast<size_t>(tiles) * kBins * passes);
+    e = cudaMemsetAsync(scratch, 0, used, stream);
     if (e != cudaSuccess) return e;
     int hist_blocks = static_cast<int>((n + 8191) / 8192);
     if (hist_blocks > 1024) hist_blocks = 1024;
-    histogram_kernel<<<hist_blocks, kSortThreads, 0, stream>>>(keys, n, hist);
-    histogram_scan_kernel<<<kPasses, kBins, 0, stream>>>(hist);
-    e = cudaFuncSetAttribute(onesweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(sizeof(SortSmem)));
-    if (e != cudaSuccess) return e;
+    histogram_kernel<<<hist_blocks, kSortThreads, 0, stream>>>(keys, n, passes, hist);
+    histogram_scan_kernel<<<passes, kBins, 0, stream>>>(hist);
     uint64_t *ki = keys, *ko = keys_alt;
     uint32_t *vi = vals, *vo = vals_alt;
-    for (int p = 0; p < kPasses; ++p) {
+    for (int p = 0; p < passes; ++p) {
         onesweep_kernel<<<static_cast<unsigned>(tiles), kSortThreads, sizeof(SortSmem), stream>>>(
             ki, vi, ko, vo, n, p, hist + p * kBins, counters + p, desc + static_cast<int64_t>(p) * tiles * kBins,
             status);
         uint64_t *tk = ki; ki = ko; ko = tk;
         uint32_t *tv = vi; vi = vo; vo = tv;
     }
-    *result_in_alt = (ki == keys_alt) ? 1 : 0;  // after 8 passes the result is back in `keys`
+    *result_in_alt = (ki == keys_alt) ? 1 : 0;  // an odd pass count leaves the result in the alternates
     return cudaGetLastError();
 }
 

@@ -78,6 +78,21 @@ SIGNATURES = {
     "nbody_set_integrator": (_i, [_vp, _i]),
     "nbody_init_device": (_i, [_vp, _i, ctypes.c_uint64, ctypes.POINTER(_f), _i]),
     "nbody_download_masses": (_i, [_vp, _vp]),
+    "nbody_ensemble_create": (_i, [ctypes.POINTER(_vp), _i, _i64]),
+    "nbody_ensemble_destroy": (_i, [_vp]),
+    "nbody_ensemble_last_error": (ctypes.c_char_p, [_vp]),
+    "nbody_ensemble_set_stream": (_i, [_vp, _vp]),
+    "nbody_ensemble_set_options": (_i, [_vp, _i, _i]),
+    "nbody_ensemble_add": (_i, [_vp, _i64, _f, _f, _f, _i, _i, _ip]),
+    "nbody_ensemble_remove": (_i, [_vp, _i]),
+    "nbody_ensemble_system_info": (_i, [_vp, _i, _ip, ctypes.POINTER(_i64)]),
+    "nbody_ensemble_upload": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
+    "nbody_ensemble_init_device": (_i, [_vp, _i, _i, ctypes.c_uint64, ctypes.POINTER(_f), _i]),
+    "nbody_ensemble_step": (_i, [_vp, _i, _i]),
+    "nbody_ensemble_download": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
+    "nbody_ensemble_sync": (_i, [_vp]),
+    "nbody_ensemble_counts": (_i, [_vp, _ip, ctypes.POINTER(_i64), ctypes.POINTER(_i64), _ip]),
+    "nbody_ensemble_footprint": (_i64, [_i64, _i]),
 }
 
 
@@ -346,3 +361,6 @@ class ParticleSolverCUDA:
         if rc != OK:
             detail = lib().nbody_last_error(self._ctx).decode() if self._ctx else ""
             raise NBodyError(rc, where, detail)
+
+
+from .ensemble import Ensemble  # noqa: E402  (uses the names above)
