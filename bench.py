@@ -1,6 +1,6 @@
 """Benchmark of the per-step gravity solve on GB300; prints ONE JSON line.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload bh|pp] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload bh|discs|pp|ensemble] [--impl ours|reference]
 
 Workloads (seeded synthetic inputs with the shapes the configurations name;
 no public dataset is involved):
@@ -16,6 +16,13 @@ no public dataset is involved):
   pp : direct sum, N = 16,384 bodies uniform in a ball of radius 100, masses
        U[1, 10), v = 0, dt = 0.0035, eps^2 = 40 (the reference's -v 2 path).
        Metric: interactions/s (N^2 per step, 20 flop each by convention).
+
+  ensemble: 2,048 independent Plummer clusters (a = 50, m = 1), N log-uniform
+       in [256, 131072]; direct sum below the autotuned crossover, Barnes-Hut
+       (theta = 0.5) above; eps^2 = 40, dt = 0.0035; steps replayed from CUDA
+       graphs. Metric: sims/s (a sim = one system for 50 steps), beside the
+       same systems stepped one at a time by the single-system solver. The
+       default line nests it as "ensemble".
 
 A "step" is one ParticleSolver::updateParticlePositions: forces + integrator.
 value: K steps on HBM-resident state, timed with CUDA events on the launch
@@ -62,6 +69,10 @@ BH_STAGE_BYTES = {"bh_bbox": 16, "bh_morton": 28, "bh_sort": 200, "bh_gather": 1
                   "bh_upsweep": 48}
 FLOP_PER_INTERACTION = 20
 L2_FLUSH_BYTES = 256 << 20
+# Batched ragged ensemble: 2,048 Plummer clusters (a = 50, m = 1, truncated at
+# 20 a), N log-uniform in [256, 131072]; a "sim" is one system run for 50 steps.
+ENS_COUNT, ENS_LO, ENS_HI, ENS_STEPS, ENS_GRAPH = 2048, 256, 131072, 50, 10
+ENS_PLUMMER = (50.0, 1.0, 20.0)
 
 
 def peaks():
@@ -373,7 +384,7 @@ def bench_bh(args, world, rank, local, dist):
         stages[name] = st
     roofline = {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(fp32, 3), "unit": "TFLOP/s",
                 "frac": round(achieved / fp32, 4), "traffic": profile_traffic("bh_traverse"),
-                "kernel": "traverse_kernel", "kernel_ms_per_launch": round(t_launch * 1e3, 4),
+                "kernel": "traverse2_kernel", "kernel_ms_per_launch": round(t_launch * 1e3, 4),
                 "work": {"pair_evaluations_per_step": pairs, "per_body": round(pairs / n, 1),
                          "warp_record_visits_per_step": visits,
                          "pair_evaluations_per_warp_visit": round(pairs / max(1, visits), 2)},
@@ -418,6 +429,185 @@ def bench_bh(args, world, rank, local, dist):
     solver.close()
     torch.cuda.set_stream(torch.cuda.default_stream())
     return line
+
+
+# ------------------------------------------------------------ ensemble (ours)
+def bench_ensemble(args, world, rank, local, dist, steps=None):
+    import torch
+
+    import nbody_gb300 as nb
+    from nbody_gb300 import autotune
+    from nbody_gb300 import initializers as I
+
+    torch.cuda.set_device(local)
+    K = int(steps or args.steps)
+    G = min(ENS_GRAPH, K)
+    sizes = I.ragged_sizes(ENS_COUNT, ENS_LO, ENS_HI, seed=2024 + rank)
+    total = int(sizes.sum())
+    t_tune = time.perf_counter()
+    tune = autotune.load_or_tune(local)
+    t_tune = time.perf_counter() - t_tune
+    X, shape = int(tune["crossover"]), tune["pp_shape"]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ens = nb.Ensemble(crossover=X, device=local, pp_shape=shape)
+    ens.set_stream(stream.cuda_stream)
+    ids = []
+    for s_, n in enumerate(sizes):
+        sid = ens.add(int(n), BH_DT, BH_EPS2, BH_THETA2)
+        ens.init_device(sid, "plummer", seed=7000 + s_, params=ENS_PLUMMER)
+        ids.append(sid)
+    counts = ens.counts()
+    pp_sizes = sizes[sizes < X]
+    # initial states on the host (pinned), for the end-to-end pass
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    host0 = []
+    for sid in ids:
+        h = ens.download(sid)
+        h.positions, h.velocities, h.accelerations, h.masses = (pin(h.positions), pin(h.velocities),
+                                                                pin(h.accelerations), pin(h.masses))
+        host0.append(h)
+
+    ens.step(2 * G, G)  # warm-up; captures the graphs of both buffer parities
+    ens.sync()
+    sampler = ClockSampler(local)
+    sampler.start()
+    t_end = time.time() + 1.0
+    while time.time() < t_end:
+        ens.step(G, G)
+        ens.sync()
+    barrier(dist)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    ens.step(K, G)
+    b.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks = sampler.stop()
+    ens.sync()
+    ms = max_over_ranks(dist, a.elapsed_time(b))
+    sec = ms / 1e3
+    value = ENS_COUNT * world * K / ENS_STEPS / sec
+
+    # per-stage times of one eager step (direct sum on the side stream, concurrent)
+    ens.profile_enable(True)
+    ens.step(2)
+    prof = ens.profile_read()
+    ens.profile_enable(False)
+    pk = peaks()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32 = fp32_peak_tflops(sms, float(pk.get("sm_max_mhz", 2070.0)))
+    pp_ms, pp_cnt = prof.get("pp_force", (0.0, 0))
+    pp_launch = pp_ms / 1e3 / max(1, pp_cnt)
+    pp_pairs = float(np.sum(pp_sizes.astype(np.float64) ** 2))
+    pp_tf = FLOP_PER_INTERACTION * pp_pairs / pp_launch / 1e12 if pp_launch > 0 else 0.0
+    bh_ms = sum(v[0] / max(1, v[1]) for k_, v in prof.items() if k_.startswith("bh_"))
+    roofline = {"bound": "fp32", "achieved": round(pp_tf, 3), "peak": round(fp32, 3), "unit": "TFLOP/s",
+                "frac": round(pp_tf / fp32, 4), "traffic": None, "kernel": "pp_batch_kernel",
+                "kernel_ms_per_launch": round(pp_launch * 1e3, 4),
+                "note": "the batched direct-sum kernel over the systems below the crossover (sum of N^2 pairs, "
+                        "20 flop each); the Barnes-Hut stages of the other systems run beside it",
+                "stages_ms_per_step": {k_: round(v[0] / max(1, v[1]), 4) for k_, v in prof.items()},
+                "bh_stages_ms_per_step": round(bh_ms, 4)}
+
+    # end to end through the public API: upload every system from pinned host
+    # arrays, K steps, download every system
+    out = [nb.ParticleSystem(*(pin(np.zeros((int(n), 4), np.float32)) for _ in range(2)),
+                             pin(np.zeros((int(n), 4), np.float32)), pin(np.zeros((int(n), 4), np.float32)))
+           for n in sizes]
+    barrier(dist)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for sid, h in zip(ids, host0):
+        ens.upload(sid, h)
+    ens.step(K, G)
+    for sid, o in zip(ids, out):
+        ens.download(sid, o)
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e = {"value": ENS_COUNT * world * K / ENS_STEPS / e2e_s, "unit": "sims/s",
+           "h2d_bytes_per_step": int(4 * 16 * total / K), "d2h_bytes_per_step": int(4 * 16 * total / K),
+           "seconds": round(e2e_s, 3),
+           "api": "nbody_ensemble_upload x 2048, nbody_ensemble_step, nbody_ensemble_download x 2048"}
+    launches = counts["launches_per_step"]
+    ens.close()
+
+    # the plain solver called one system at a time on the same GPU (same stream)
+    k_plain = min(K, 10)
+    solvers = []
+    for s_, n in enumerate(sizes):
+        mode = "pp" if n < X else "bh"
+        sv = nb.ParticleSolverCUDA(BH_DT, BH_EPS2, int(n), mode=mode, theta2=BH_THETA2, device=local)
+        sv.set_stream(stream.cuda_stream)
+        sv.init_device("plummer", seed=7000 + s_, params=ENS_PLUMMER)
+        solvers.append(sv)
+    for sv in solvers:
+        sv.step(1)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for sv in solvers:
+        sv.step(k_plain)
+    b.record(stream)
+    torch.cuda.synchronize()
+    for sv in solvers:
+        sv.sync()
+    plain_s = a.elapsed_time(b) / 1e3
+    t_w = time.perf_counter()
+    for sv in solvers:
+        sv.step(k_plain)
+    torch.cuda.synchronize()
+    plain_wall = time.perf_counter() - t_w
+    for sv in solvers:
+        sv.close()
+    plain = {"value": ENS_COUNT * k_plain / ENS_STEPS / plain_s, "unit": "sims/s",
+             "wall_value": ENS_COUNT * k_plain / ENS_STEPS / plain_wall, "steps_per_system": k_plain,
+             "how": "2048 single-system solvers (nbody_create, mode by the same crossover) on one stream, each "
+                    "stepped k times before the next; CUDA events around the whole loop"}
+    line = {"metric": METRIC, "component": "batched ensemble sims/s", "value": value, "unit": "sims/s",
+            "n_gpus": world, "steps": K, "warmup": 2 * G, "ms_per_step": ms / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batched ragged ensemble: 2048 Plummer clusters (a=50, m=1, truncated at 20a), "
+                                   "N log-uniform in [256, 131072] (seed 2024); direct sum below the tuned "
+                                   "crossover, Barnes-Hut theta=0.5 above; eps2=40, dt=0.0035; a sim = one system "
+                                   "for 50 steps", "systems": ENS_COUNT, "bodies": total,
+                       "crossover": X, "pp_shape": shape, "graph_steps": G,
+                       "pp_systems": int(len(pp_sizes)), "bh_systems": int(ENS_COUNT - len(pp_sizes)),
+                       "tuning": {k_: tune[k_] for k_ in ("source", "tuned_at") if k_ in tune},
+                       "tuning_seconds": round(t_tune, 2), "parallelism": "replicas",
+                       "l2": f"inputs larger than L2 ({total * 16 / 1e9:.2f} GB of positions)"},
+            "body_steps_per_s": total * world * K / sec, "clocks": clocks, "roofline": roofline, "e2e": e2e,
+            "plain_loop": plain, "speedup_vs_plain": round(value / plain["value"], 3),
+            "gpu_launches": launches * K}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_ensemble(sizes, X)
+    torch.cuda.set_stream(torch.cuda.default_stream())
+    return line
+
+
+def cpu_baseline_ensemble(sizes, crossover, sample: int = 24, seed: int = 3):
+    """The port on a random sample of the systems, one step each, scaled to the ensemble."""
+    import pyoracle
+    from nbody_gb300 import initializers as I
+
+    pyoracle.build(reference=False)
+    threads = cpu_threads()
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(len(sizes), size=min(sample, len(sizes)), replace=False)
+    secs = 0.0
+    for j in pick:
+        n = int(sizes[j])
+        pos, vel, mass = I.plummer(n, a=ENS_PLUMMER[0], seed=int(j))
+        acc = np.zeros_like(pos)
+        if n < crossover:
+            secs += pyoracle.pp_run(pos, vel, acc, mass, BH_DT, BH_EPS2, 1, threads=threads)[4]
+        else:
+            secs += pyoracle.bh_run(pos, vel, acc, mass, BH_DT, BH_EPS2, 1, theta2=BH_THETA2, threads=threads,
+                                    patched=True)[4]["seconds"]
+    per_step_all = secs * len(sizes) / len(pick)
+    return {"value": 1.0 / (per_step_all * ENS_STEPS), "unit": "sims/s", "cores": threads, "kind": "port",
+            "sample": f"one step of each of {len(pick)} randomly chosen systems (-v 2 / -v 6 restated, {threads} "
+                      f"threads), scaled to 2048 systems x 50 steps"}
 
 
 def cpu_baseline_bh(budget_s: float = 15.0):
@@ -529,10 +719,11 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", choices=["bh", "discs", "pp"], default="bh")
+    ap.add_argument("--workload", choices=["bh", "discs", "pp", "ensemble"], default="bh")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-pp", action="store_true", help="leave the nested direct-sum measurement out")
+    ap.add_argument("--no-ensemble", action="store_true", help="leave the nested ensemble measurement out")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_env()
@@ -549,6 +740,8 @@ def main():
     dist = init_dist(world, local)
     if args.workload == "pp":
         line = bench_pp(args, world, rank, local, dist)
+    elif args.workload == "ensemble":
+        line = bench_ensemble(args, world, rank, local, dist)
     else:
         line = bench_bh(args, world, rank, local, dist)
         if not args.no_pp and args.workload == "bh":
@@ -558,6 +751,12 @@ def main():
             line["pp"] = {k: pp[k] for k in ("component", "value", "unit", "steps", "ms_per_step", "roofline",
                                              "e2e", "clocks", "gpu_launches", "config", "cpu_baseline")
                           if k in pp}
+        if not args.no_ensemble and args.workload == "bh":
+            en = bench_ensemble(args, world, rank, local, dist, steps=ENS_STEPS)
+            line["ensemble"] = {k: en[k] for k in ("component", "value", "unit", "steps", "ms_per_step", "roofline",
+                                                   "e2e", "clocks", "gpu_launches", "config", "plain_loop",
+                                                   "speedup_vs_plain", "body_steps_per_s", "cpu_baseline")
+                                if k in en}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

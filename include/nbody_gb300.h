@@ -271,6 +271,11 @@ int nbody_ensemble_sync(nbody_ensemble *e);
 /* Live systems, bodies per group, and kernel launches per step. */
 int nbody_ensemble_counts(nbody_ensemble *e, int *systems, int64_t *pp_bodies, int64_t *bh_bodies,
                           int *launches_per_step);
+/* Per-stage CUDA-event timing as nbody_profile_enable / nbody_profile_read
+ * (stage names from nbody_stage_name); while it is on, steps run without
+ * graphs. The direct-sum stage is timed on the side stream. */
+int nbody_ensemble_profile_enable(nbody_ensemble *e, int on);
+int nbody_ensemble_profile_read(nbody_ensemble *e, double *ms, int *launches, int nstages);
 /* Device bytes one system of n bodies takes in an ensemble (for admission). */
 int64_t nbody_ensemble_footprint(int64_t n, int mode);
 

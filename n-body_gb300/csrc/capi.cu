@@ -21,62 +21,7 @@
 #include "kernels.h"
 #include "nbody_gb300.h"
 #include "sort.h"
-
-namespace {
-
-// Records a CUDA event pair around each launcher stage on the launch stream;
-// read back (and reset) by nbody_profile_read.
-struct EventTimer : nbody::StageTimer {
-    struct Rec {
-        int stage;
-        cudaEvent_t a, b;
-    };
-    std::vector<cudaEvent_t> pool;
-    size_t used = 0;
-    std::vector<Rec> recs;
-    cudaEvent_t open[nbody::kStageCount] = {};
-
-    cudaEvent_t get() {
-        if (used == pool.size()) {
-            cudaEvent_t e = nullptr;
-            if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
-            pool.push_back(e);
-        }
-        return pool[used++];
-    }
-    void begin(int st, cudaStream_t s) override {
-        cudaEvent_t e = get();
-        if (e) cudaEventRecord(e, s);
-        open[st] = e;
-    }
-    void end(int st, cudaStream_t s) override {
-        cudaEvent_t e = get();
-        if (e) cudaEventRecord(e, s);
-        if (e && open[st]) recs.push_back({st, open[st], e});
-        open[st] = nullptr;
-    }
-    cudaError_t read(double *ms, int *count, int nstages) {
-        for (const Rec &r : recs) {
-            cudaError_t e = cudaEventSynchronize(r.b);
-            if (e != cudaSuccess) return e;
-            float t = 0.f;
-            e = cudaEventElapsedTime(&t, r.a, r.b);
-            if (e != cudaSuccess) return e;
-            if (r.stage < nstages) {
-                if (ms) ms[r.stage] += t;
-                if (count) count[r.stage] += 1;
-            }
-        }
-        recs.clear();
-        used = 0;
-        return cudaSuccess;
-    }
-    ~EventTimer() override {
-        for (cudaEvent_t e : pool) cudaEventDestroy(e);
-    }
-};
-
-}  // namespace
+#include "timer.h"
 
 struct nbody_ctx {
     int device = 0;
@@ -94,7 +39,7 @@ struct nbody_ctx {
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     bool uploaded = false;
-    EventTimer *timer = nullptr;  // non-null while profiling is enabled
+    nbody::EventTimer *timer = nullptr;  // non-null while profiling is enabled
     std::string last_error;
 
     // Barnes-Hut resident state, kept in the order of the last sort: pos[bh_pos],
@@ -623,7 +568,7 @@ int nbody_profile_enable(nbody_ctx *ctx, int on) {
     if (!ctx) return NBODY_ERR_ARG;
     DeviceGuard dg(ctx->device);
     if (on && !ctx->timer) {
-        ctx->timer = new (std::nothrow) EventTimer();
+        ctx->timer = new (std::nothrow) nbody::EventTimer();
         if (!ctx->timer) return NBODY_ERR_NOMEM;
     } else if (!on && ctx->timer) {
         NB_CK(ctx, cudaStreamSynchronize(ctx->stream));

@@ -34,6 +34,7 @@
 #include "nbody_gb300.h"
 #include "pp_batch.h"
 #include "sort.h"
+#include "timer.h"
 
 namespace {
 
@@ -122,6 +123,7 @@ struct nbody_ensemble {
     };
     std::map<std::tuple<int, int, int>, Graph> graphs;
     int64_t steps_done = 0;
+    nbody::EventTimer *timer = nullptr;  // non-null while profiling (steps then run without graphs)
 };
 
 namespace {
@@ -410,16 +412,18 @@ int step_once(nbody_ensemble *e) {
     if (e->pp_nitems > 0) {
         EN_CK(e, cudaEventRecord(e->fork, e->stream));
         EN_CK(e, cudaStreamWaitEvent(e->side, e->fork, 0));
+        if (e->timer) e->timer->begin(nbody::kStagePPForce, e->side);
         EN_CK(e, nbody::pp_batch_launch(e->pp_shape, e->pp_ctas, e->pp_pos[e->pp_cur], e->pp_pos[e->pp_cur ^ 1],
                                         e->pp_vel, e->pp_acc, e->pp_items, e->pp_nitems, e->pp_range, e->pp_prm,
                                         e->pp_sched, e->side, e->status));
+        if (e->timer) e->timer->end(nbody::kStagePPForce, e->side);
         e->pp_cur ^= 1;
     }
     if (e->bh_n > 0) {
         const int va = e->bh_va;
         EN_CK(e, nbody::bh_ensemble_step(e->bh_n, e->ws, e->tab, e->key_mode, e->bh_pos[0], e->bh_pos[1],
                                          e->bh_vel[va], e->bh_vel[va ^ 1], e->bh_acc[va], e->bh_acc[va ^ 1],
-                                         e->bh_ids[va], e->bh_ids[va ^ 1], e->stream, e->status, nullptr));
+                                         e->bh_ids[va], e->bh_ids[va ^ 1], e->stream, e->status, e->timer));
         e->bh_va ^= 1;
     }
     if (e->pp_nitems > 0) {
@@ -513,6 +517,8 @@ int nbody_ensemble_destroy(nbody_ensemble *e) {
         if (e->side) cudaStreamSynchronize(e->side);
         if (e->stream) cudaStreamSynchronize(e->stream);
         clear_graphs(e);
+        delete e->timer;
+        e->timer = nullptr;
         if (e->pool && e->stream) {
             free_layout(e);
             cudaStreamSynchronize(e->stream);
@@ -648,7 +654,7 @@ int nbody_ensemble_step(nbody_ensemble *e, int steps, int graph_steps) {
     for (const Sys &s : e->sys)
         if (s.alive && !s.ready) return NBODY_ERR_STATE;
     int left = steps;
-    if (graph_steps > 0)
+    if (graph_steps > 0 && !e->timer)
         while (rc == NBODY_OK && left >= graph_steps) {
             rc = run_graph(e, graph_steps);
             left -= graph_steps;
@@ -735,6 +741,33 @@ int nbody_ensemble_counts(nbody_ensemble *e, int *systems, int64_t *pp_bodies, i
             l += 2 + (2 + 8) + (e->tab.systems > 1 ? 3 + e->tab.seg_passes : 0) + 1 + 9 + 1;
         *launches_per_step = l;
     }
+    return NBODY_OK;
+}
+
+int nbody_ensemble_profile_enable(nbody_ensemble *e, int on) {
+    if (!e) return NBODY_ERR_ARG;
+    if (on && !e->timer) {
+        e->timer = new (std::nothrow) nbody::EventTimer();
+        if (!e->timer) return NBODY_ERR_NOMEM;
+    } else if (!on && e->timer) {
+        DevGuard dg(e->device);
+        cudaStreamSynchronize(e->stream);
+        cudaStreamSynchronize(e->side);
+        delete e->timer;
+        e->timer = nullptr;
+    }
+    return NBODY_OK;
+}
+
+int nbody_ensemble_profile_read(nbody_ensemble *e, double *ms, int *launches, int nstages) {
+    if (!e || nstages < 0) return NBODY_ERR_ARG;
+    for (int k = 0; k < nstages; ++k) {
+        if (ms) ms[k] = 0.0;
+        if (launches) launches[k] = 0;
+    }
+    if (!e->timer) return NBODY_OK;
+    DevGuard dg(e->device);
+    EN_CK(e, e->timer->read(ms, launches, nstages));
     return NBODY_OK;
 }
 

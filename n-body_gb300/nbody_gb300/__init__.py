@@ -93,6 +93,8 @@ SIGNATURES = {
     "nbody_ensemble_sync": (_i, [_vp]),
     "nbody_ensemble_counts": (_i, [_vp, _ip, ctypes.POINTER(_i64), ctypes.POINTER(_i64), _ip]),
     "nbody_ensemble_footprint": (_i64, [_i64, _i]),
+    "nbody_ensemble_profile_enable": (_i, [_vp, _i]),
+    "nbody_ensemble_profile_read": (_i, [_vp, ctypes.POINTER(ctypes.c_double), _ip, _i]),
 }
 
 

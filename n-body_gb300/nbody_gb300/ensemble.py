@@ -96,6 +96,18 @@ class Ensemble:
                                                 ctypes.byref(l)), "nbody_ensemble_counts")
         return {"systems": s.value, "pp_bodies": p.value, "bh_bodies": b.value, "launches_per_step": l.value}
 
+    def profile_enable(self, on: bool = True) -> None:
+        """Per-stage CUDA-event timing (steps then run without graphs)."""
+        self._check(lib().nbody_ensemble_profile_enable(self._e, int(on)), "nbody_ensemble_profile_enable")
+
+    def profile_read(self) -> dict:
+        """{stage name: (milliseconds, launches)} since the last read."""
+        k = lib().nbody_stage_count()
+        ms = (ctypes.c_double * k)()
+        cnt = (ctypes.c_int * k)()
+        self._check(lib().nbody_ensemble_profile_read(self._e, ms, cnt, k), "nbody_ensemble_profile_read")
+        return {lib().nbody_stage_name(i).decode(): (ms[i], cnt[i]) for i in range(k) if cnt[i]}
+
     @staticmethod
     def footprint(n: int, mode) -> int:
         return int(lib().nbody_ensemble_footprint(int(n), _MODES[mode]))

@@ -142,6 +142,12 @@ def lagrange(world=(5.0, 5.0, 5.0), G: float = 1.0):
     return pos, vel, np.full(3, mass, np.float32)
 
 
+def ragged_sizes(count: int = 2048, lo: int = 256, hi: int = 131072, seed: int = 2024) -> np.ndarray:
+    """System sizes log-uniform in [lo, hi] (the batched-ensemble workload)."""
+    rng = np.random.default_rng(seed)
+    return np.minimum(hi, np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1), count)))).astype(np.int64)
+
+
 def pos_mass(pos4: np.ndarray, mass: np.ndarray) -> np.ndarray:
     """Device layout: (x, y, z, m) per body."""
     out = np.array(pos4, dtype=np.float32, copy=True)
