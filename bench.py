@@ -585,6 +585,80 @@ def bench_ensemble(args, world, rank, local, dist, steps=None):
     return line
 
 
+# ------------------------------------------------------------- serving (ours)
+SERVE_BUDGET = 150e9
+
+
+def bench_serving(args, world, rank, local, dist, rates=(10.0, 100.0, 1000.0), count=None):
+    import torch
+
+    import nbody_gb300 as nb  # noqa: F401  (loads the library)
+    from nbody_gb300 import autotune, serving
+
+    torch.cuda.set_device(local)
+    tune = autotune.load_or_tune(local)
+    X, shape = int(tune["crossover"]), tune["pp_shape"]
+    count = int(count or args.requests)
+    per_rate = []
+    for rate in rates:
+        reqs = serving.poisson_trace(count, rate=rate, seed=11 + rank)
+        with serving.Server(budget_bytes=SERVE_BUDGET, device=local, crossover=X, pp_shape=shape,
+                            max_chunk=10) as srv:
+            # warm-up request (module load, first allocations), untimed
+            srv.run_trace([serving.Request(rid=-1, n=4096, steps=3, dt=0.001, eps2=10.0)], realtime=False)
+            sampler = ClockSampler(local)
+            sampler.start()
+            served = srv.run_trace(reqs, realtime=True)
+            clocks = sampler.stop()
+            stats = srv.stats
+        plain = serving.run_fifo_plain(reqs, device=local, crossover=X, realtime=True)
+        # each served result against the same request run alone by the plain solver
+        bh_equal, pp_err = 0, 0.0
+        n_bh = 0
+        for r in reqs:
+            a, b = served[r.rid], plain[r.rid]
+            if not (a.ok and b.ok):
+                continue
+            if a.mode == "bh":
+                n_bh += 1
+                bh_equal += int(np.array_equal(a.system.positions, b.system.positions) and
+                                np.array_equal(a.system.velocities, b.system.velocities))
+            else:
+                ga, gb = a.system.accelerations[:, :3], b.system.accelerations[:, :3]
+                rel = np.linalg.norm(ga - gb, axis=1) / np.maximum(np.linalg.norm(gb, axis=1), 1e-30)
+                pp_err = max(pp_err, float(np.sqrt(np.mean(rel ** 2))))
+        s_sum, p_sum = serving.summarize(served, reqs), serving.summarize(plain, reqs)
+        per_rate.append({"rate_req_per_s": rate, "served": s_sum, "plain_fifo": p_sum,
+                         "speedup_sims_per_s": round(s_sum["sims_per_s"] / max(1e-12, p_sum["sims_per_s"]), 3),
+                         "p99_ratio_plain_over_served": round(p_sum["p99_latency_s"] /
+                                                              max(1e-12, s_sum["p99_latency_s"]), 3),
+                         "max_in_flight": stats.max_in_flight, "chunks": stats.chunks,
+                         "peak_footprint_gb": round(stats.peak_footprint / 1e9, 2),
+                         "gpu_busy_frac": round(stats.busy_seconds / max(1e-9, s_sum["makespan_s"]), 3),
+                         "bh_requests_bit_equal_alone": f"{bh_equal}/{n_bh}",
+                         "pp_requests_max_accel_rms_rel_vs_alone": pp_err, "clocks": clocks})
+    head = max(per_rate, key=lambda d: d["rate_req_per_s"])
+    body_steps = sum(r.n * r.steps for r in serving.poisson_trace(count, rate=head["rate_req_per_s"], seed=11 + rank))
+    return {"metric": METRIC, "component": "served sims/s", "value": head["served"]["sims_per_s"] * world,
+            "unit": "sims/s", "n_gpus": world, "steps": None, "warmup": 1, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"serving: {count} requests per rate, Poisson arrivals; Plummer a=100 or uniform "
+                                   f"ball R=100, N log-uniform in [1024, 4194304], steps U[10, 500], dt in "
+                                   f"{{0.001, 0.0035}}, eps2 U[10, 40], theta=0.5; admission by HBM footprint under "
+                                   f"150 GB; continuous batching in chunks of <= 10 steps", "requests": count,
+                       "rates": list(rates), "crossover": X, "pp_shape": shape,
+                       "body_steps_per_trace": int(body_steps), "parallelism": "replicas"},
+            "p50_latency_s": head["served"]["p50_latency_s"], "p99_latency_s": head["served"]["p99_latency_s"],
+            "plain_fifo": head["plain_fifo"], "speedup_vs_plain": head["speedup_sims_per_s"],
+            "per_rate": per_rate, "clocks": head["clocks"],
+            "e2e": {"value": head["served"]["sims_per_s"] * world, "unit": "sims/s",
+                    "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(sum(4 * 16 * r.n for r in serving.poisson_trace(count, rate=1.0,
+                                                                                               seed=11 + rank))),
+                    "note": "requests are generated on the device from their seeds; every result is downloaded "
+                            "(4 vec4 arrays) before it counts as complete, inside the measured latency"}}
+
+
 def cpu_baseline_ensemble(sizes, crossover, sample: int = 24, seed: int = 3):
     """The port on a random sample of the systems, one step each, scaled to the ensemble."""
     import pyoracle
@@ -719,7 +793,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", choices=["bh", "discs", "pp", "ensemble"], default="bh")
+    ap.add_argument("--workload", choices=["bh", "discs", "pp", "ensemble", "serving"], default="bh")
+    ap.add_argument("--requests", type=int, default=32, help="requests per rate of the serving workload")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-pp", action="store_true", help="leave the nested direct-sum measurement out")
@@ -742,6 +817,8 @@ def main():
         line = bench_pp(args, world, rank, local, dist)
     elif args.workload == "ensemble":
         line = bench_ensemble(args, world, rank, local, dist)
+    elif args.workload == "serving":
+        line = bench_serving(args, world, rank, local, dist)
     else:
         line = bench_bh(args, world, rank, local, dist)
         if not args.no_pp and args.workload == "bh":

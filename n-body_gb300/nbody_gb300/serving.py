@@ -1,0 +1,278 @@
+"""Serving: a request loop with continuous batching over an ensemble.
+
+A request carries an initial state (explicit host arrays, or a seeded
+generator run on the device), N, dt, eps^2, theta and a step count. The server
+keeps every admitted request's state resident in HBM inside one Ensemble,
+admits waiting requests in arrival order while their device footprint fits the
+memory budget, steps all admitted requests together in chunks of at most
+`max_chunk` steps (a chunk never runs past the soonest finish), and between
+chunks retires finished requests (download, remove) and folds new arrivals
+into the next launch. A request's result does not depend on what else was in
+flight: ensembles compute every system on its own.
+
+`run_fifo_plain` is the comparison point: the single-system solver
+(nbody_create) serving the same requests one at a time in arrival order.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import NBodyError, ParticleSolverCUDA, ParticleSystem
+from .ensemble import Ensemble
+
+
+@dataclass
+class Request:
+    rid: int
+    n: int
+    steps: int
+    dt: float
+    eps2: float
+    theta2: float = 0.25
+    init: str = "plummer"            # a device initialiser kind, or "state"
+    params: tuple | None = None      # initialiser parameters
+    seed: int = 0
+    state: ParticleSystem | None = None  # explicit initial state (init == "state")
+    arrival: float = 0.0             # seconds after the start of the trace
+
+
+@dataclass
+class Result:
+    rid: int
+    ok: bool
+    mode: str = ""
+    system: ParticleSystem | None = None
+    error: str = ""
+    arrival: float = 0.0
+    admitted: float = 0.0
+    completed: float = 0.0
+
+    @property
+    def latency(self) -> float:
+        return self.completed - self.arrival
+
+
+@dataclass
+class _Active:
+    req: Request
+    sid: int
+    left: int
+    footprint: int
+    admitted: float
+    mode: str = ""
+
+
+@dataclass
+class ServerStats:
+    chunks: int = 0
+    steps: int = 0
+    relayouts: int = 0
+    max_in_flight: int = 0
+    peak_footprint: int = 0
+    busy_seconds: float = 0.0
+    in_flight_samples: list = field(default_factory=list)
+
+
+def percentile(xs, q) -> float:
+    return float(np.percentile(np.asarray(xs, np.float64), q)) if len(xs) else float("nan")
+
+
+class Server:
+    def __init__(self, budget_bytes: float = 150e9, device: int = 0, crossover: int | None = None,
+                 pp_shape: str | None = None, max_chunk: int = 10, keep_results: bool = True, ensemble=None):
+        """`ensemble` replaces the device ensemble (any object with the
+        Ensemble methods; used to test the loop without a GPU)."""
+        if ensemble is not None and crossover is None:
+            crossover = ensemble.crossover
+        if ensemble is None and (crossover is None or pp_shape is None):
+            from .autotune import load_or_tune
+
+            t = load_or_tune(device)
+            crossover = t["crossover"] if crossover is None else crossover
+            pp_shape = t["pp_shape"] if pp_shape is None else pp_shape
+        self.budget = int(budget_bytes)
+        self.crossover = int(crossover)
+        self.max_chunk = int(max_chunk)
+        self.keep_results = keep_results
+        self.ens = ensemble if ensemble is not None else Ensemble(crossover=self.crossover, device=device,
+                                                                  pp_shape=pp_shape)
+        self.stats = ServerStats()
+
+    def close(self) -> None:
+        self.ens.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def footprint(self, req: Request) -> int:
+        mode = "pp" if req.n < self.crossover else "bh"
+        # a re-layout holds the old and the new packed state for a moment
+        return 2 * self.ens.footprint(req.n, mode)
+
+    def _admit(self, req: Request, now: float) -> _Active:
+        ens = self.ens
+        sid = ens.add(req.n, req.dt, req.eps2, req.theta2)
+        try:
+            if req.init == "state":
+                if req.state is None or req.state.n != req.n:
+                    raise ValueError("request state missing or of the wrong size")
+                ens.upload(sid, req.state)
+            else:
+                ens.init_device(sid, req.init, seed=req.seed, params=req.params)
+        except Exception:
+            ens.remove(sid)
+            raise
+        return _Active(req, sid, req.steps, self.footprint(req), now, ens.info(sid)[0])
+
+    def run_trace(self, requests, realtime: bool = True, clock=time.perf_counter):
+        """Serves `requests` (arrival times relative to the start). With
+        realtime, a request becomes visible when the wall clock passes its
+        arrival; otherwise all are visible at once. Returns results by rid."""
+        pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
+        queue: list[Request] = []
+        active: list[_Active] = []
+        results: dict[int, Result] = {}
+        used = 0
+        t0 = clock()
+        now = lambda: clock() - t0  # noqa: E731
+        st = self.stats
+        while pending or queue or active:
+            t = now()
+            while pending and (not realtime or pending[0].arrival <= t):
+                queue.append(pending.pop(0))
+            # admission in arrival order while the footprint fits
+            changed = False
+            while queue:
+                req = queue[0]
+                fp = self.footprint(req)
+                if fp > self.budget:
+                    queue.pop(0)
+                    results[req.rid] = Result(req.rid, False, error="larger than the memory budget",
+                                              arrival=req.arrival, admitted=t, completed=now())
+                    continue
+                if used + fp > self.budget:
+                    break
+                queue.pop(0)
+                try:
+                    act = self._admit(req, now())
+                except (NBodyError, ValueError) as e:
+                    results[req.rid] = Result(req.rid, False, error=str(e), arrival=req.arrival, admitted=now(),
+                                              completed=now())
+                    continue
+                active.append(act)
+                used += act.footprint
+                changed = True
+            if changed:
+                st.relayouts += 1
+            st.max_in_flight = max(st.max_in_flight, len(active))
+            st.peak_footprint = max(st.peak_footprint, used)
+            if not active:
+                if pending and realtime:
+                    time.sleep(max(0.0, min(0.01, pending[0].arrival - now())))
+                continue
+            k = min(self.max_chunk, min(a.left for a in active))
+            tb = clock()
+            try:
+                self.ens.step(k)
+                self.ens.sync()
+            except NBodyError as e:
+                # a failed step: every request in flight fails, the server goes on
+                for a in active:
+                    results[a.req.rid] = Result(a.req.rid, False, a.mode, error=str(e), arrival=a.req.arrival,
+                                                admitted=a.admitted, completed=now())
+                    self.ens.remove(a.sid)
+                active, used = [], 0
+                continue
+            st.busy_seconds += clock() - tb
+            st.chunks += 1
+            st.steps += k
+            st.in_flight_samples.append(len(active))
+            still = []
+            for a in active:
+                a.left -= k
+                if a.left > 0:
+                    still.append(a)
+                    continue
+                system = self.ens.download(a.sid) if self.keep_results else None
+                self.ens.remove(a.sid)
+                used -= a.footprint
+                results[a.req.rid] = Result(a.req.rid, True, a.mode, system, arrival=a.req.arrival,
+                                            admitted=a.admitted, completed=now())
+            active = still
+        return results
+
+
+def run_fifo_plain(requests, device: int = 0, crossover: int = 4096, realtime: bool = True,
+                   keep_results: bool = True, clock=time.perf_counter):
+    """The single-system solver serving the requests one at a time, in arrival order."""
+    pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
+    results: dict[int, Result] = {}
+    t0 = clock()
+    now = lambda: clock() - t0  # noqa: E731
+    for req in pending:
+        if realtime:
+            wait = req.arrival - now()
+            if wait > 0:
+                time.sleep(wait)
+        start = now()
+        mode = "pp" if req.n < crossover else "bh"
+        try:
+            s = ParticleSolverCUDA(req.dt, req.eps2, req.n, mode=mode, theta2=req.theta2, device=device)
+            try:
+                if req.init == "state":
+                    s.upload(req.state)
+                else:
+                    s.init_device(req.init, seed=req.seed, params=req.params)
+                s.step(req.steps)
+                out = None
+                if keep_results:
+                    z = np.zeros((req.n, 4), np.float32)
+                    out = ParticleSystem(z, z.copy(), np.zeros(req.n, np.float32), z.copy())
+                    s.download(out, masses=True)
+                else:
+                    s.sync()
+            finally:
+                s.close()
+            results[req.rid] = Result(req.rid, True, mode, out, arrival=req.arrival, admitted=start,
+                                      completed=now())
+        except NBodyError as e:
+            results[req.rid] = Result(req.rid, False, mode, error=str(e), arrival=req.arrival, admitted=start,
+                                      completed=now())
+    return results
+
+
+def poisson_trace(count: int, rate: float, seed: int = 11, n_lo: int = 1024, n_hi: int = 4_194_304,
+                  steps_lo: int = 10, steps_hi: int = 500):
+    """Requests of the serving workload: Poisson arrivals at `rate` per second;
+    a Plummer sphere (a = 100) or a uniform ball (R = 100), N log-uniform in
+    [n_lo, n_hi], steps uniform in [steps_lo, steps_hi], dt in {0.001,
+    0.0035}, eps^2 uniform in [10, 40], theta = 0.5."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, count))
+    out = []
+    for i in range(count):
+        n = int(min(n_hi, np.floor(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi + 1))))))
+        kind = "plummer" if rng.random() < 0.5 else "uniform_ball"
+        params = (100.0, 1.0, 20.0) if kind == "plummer" else (100.0, 1.0, 10.0)
+        out.append(Request(rid=i, n=n, steps=int(rng.integers(steps_lo, steps_hi + 1)),
+                           dt=float(rng.choice([0.001, 0.0035])), eps2=float(rng.uniform(10.0, 40.0)), theta2=0.25,
+                           init=kind, params=params, seed=1000 + i, arrival=float(t[i])))
+    return out
+
+
+def summarize(results, requests) -> dict:
+    ok = [r for r in results.values() if r.ok]
+    lat = [r.latency for r in ok]
+    first = min(r.arrival for r in requests)
+    last = max((r.completed for r in results.values()), default=first)
+    span = max(1e-9, last - first)
+    return {"requests": len(requests), "completed": len(ok), "failed": len(results) - len(ok),
+            "sims_per_s": len(ok) / span, "makespan_s": round(span, 3),
+            "p50_latency_s": round(percentile(lat, 50), 4), "p99_latency_s": round(percentile(lat, 99), 4),
+            "mean_latency_s": round(float(np.mean(lat)) if lat else float("nan"), 4)}
