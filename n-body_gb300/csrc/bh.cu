@@ -619,6 +619,39 @@ __global__ void upsweep_kernel(const uint64_t *__restrict__ k, int64_t n, const 
 // the record's `next`. The warp descends (i + 1) if any lane opened the
 // record, otherwise it jumps to the smallest `skip` of its lanes. Every lane
 // therefore sees exactly the records its own reference walk would accept.
+// Both bodies of a lane summing the same run of bodies in one packed loop;
+// side A takes part when doA, side B when doB. Per side the arithmetic and
+// its rounding are those of direct_sum_range: a side that does not take part,
+// or a pair it skips (m == 0 or r^2 == 0), adds dx * 0 = +0 to its sums.
+__device__ __forceinline__ void direct_sum_range2(const float4 *__restrict__ pos, int64_t n, int first, int count,
+                                                  float2 nx, float2 ny, float2 nz, float eps2, bool doA, bool doB,
+                                                  float &fAx, float &fAy, float &fAz, float &fBx, float &fBy,
+                                                  float &fBz) {
+    const int q0 = first < 0 ? 0 : first;
+    const int q1 = first + count < n ? first + count : static_cast<int>(n);
+    float2 ax = make_float2(fAx, fBx), ay = make_float2(fAy, fBy), az = make_float2(fAz, fBz);
+    for (int q = q0; q < q1; ++q) {
+        const float4 o = pos[q];
+        const float2 ex = __fadd2_rn(make_float2(o.x, o.x), nx);
+        const float2 ey = __fadd2_rn(make_float2(o.y, o.y), ny);
+        const float2 ez = __fadd2_rn(make_float2(o.z, o.z), nz);
+        const float2 r2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(ex, ex), __fmul2_rn(ey, ey)), __fmul2_rn(ez, ez));
+        const float2 iv = make_float2(rsqrt_ftz(r2.x + eps2), rsqrt_ftz(r2.y + eps2));
+        const float2 w = __fmul2_rn(__fmul2_rn(__fmul2_rn(make_float2(o.w, o.w), iv), iv), iv);
+        const bool ua = doA && o.w > 0.f && r2.x > 0.f, ub = doB && o.w > 0.f && r2.y > 0.f;
+        const float2 ws = make_float2(ua ? w.x : 0.f, ub ? w.y : 0.f);
+        ax = __ffma2_rn(ex, ws, ax);
+        ay = __ffma2_rn(ey, ws, ay);
+        az = __ffma2_rn(ez, ws, az);
+    }
+    fAx = ax.x;
+    fAy = ay.x;
+    fAz = az.x;
+    fBx = ax.y;
+    fBy = ay.y;
+    fBz = az.y;
+}
+
 __device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, float fy, float fz, float dt,
                                                  float4 *__restrict__ pos_out, float4 *__restrict__ vel,
                                                  float4 *__restrict__ acc, float4 *__restrict__ force_out,
@@ -785,8 +818,12 @@ __device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, 
 // of the warp, first body of the system, end of the system}, walks only the
 // system's records [P[first], P[end]) and takes dt, eps2, theta2 and the
 // integrator from params[system] = {dt, eps2, theta2, euler}.
-template <bool COUNT, bool POT, bool SEG>
-__global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict__ nodes,
+// GUARD keeps the reference's explicit d2 > 0 and leaf tests; without it
+// (eps2 > 0, no potential) they are implied: a leaf's s2 = -1 is below
+// theta2 * d2 >= 0, and a record at zero distance adds dx * w = +0 to every
+// component, so the accepted set and the sums are the same bit for bit.
+template <bool COUNT, bool POT, bool SEG, bool GUARD>
+__global__ void __launch_bounds__(256, SEG ? 5 : 6) traverse2_kernel(const BHNode *__restrict__ nodes,
                                                         const uint32_t *__restrict__ node_total,
                                                         const float4 *__restrict__ pos, int64_t n, float eps2,
                                                         float theta2, float dt, float4 *__restrict__ pos_out,
@@ -804,13 +841,13 @@ __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict
     int64_t base, end;
     int i, m_nodes;
     if (SEG) {
+        // Only what the walk needs stays live through it; the body range, dt
+        // and the integrator are read again afterwards.
         if (warp >= nwork) return;  // whole warps
         const int4 ww = work[warp];
         const float4 prm = params[ww.x];
-        dt = prm.x;
         eps2 = prm.y;
         theta2 = prm.z;
-        euler = prm.w != 0.f ? 1 : 0;
         base = ww.y;
         end = ww.w;
         i = static_cast<int>(P[ww.z]);
@@ -821,11 +858,11 @@ __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict
         i = 0;
         m_nodes = static_cast<int>(*node_total);
     }
-    const int64_t bA = base + lane, bB = bA + 32;
-    const bool vA = bA < end, vB = bB < end;
-    const float4 meA = vA ? pos[bA] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 meB = vB ? pos[bB] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float2 nx = make_float2(-meA.x, -meB.x), ny = make_float2(-meA.y, -meB.y), nz = make_float2(-meA.z, -meB.z);
+    bool vA = base + lane < end, vB = base + lane + 32 < end;
+    const float4 meA0 = vA ? pos[base + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 meB0 = vB ? pos[base + lane + 32] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 nx = make_float2(-meA0.x, -meB0.x), ny = make_float2(-meA0.y, -meB0.y),
+                 nz = make_float2(-meA0.z, -meB0.z);
     const float2 th = make_float2(theta2, theta2);
     int skipA = vA ? i : m_nodes, skipB = vB ? i : m_nodes;
     float fAx = 0.f, fAy = 0.f, fAz = 0.f, fBx = 0.f, fBy = 0.f, fBz = 0.f;
@@ -839,10 +876,20 @@ __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict
         const float2 d2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
         const float s2 = __int_as_float(meta.x);
         const float2 rhs = __fmul2_rn(th, d2);
-        const bool accA = actA && (s2 < 0.f || s2 < rhs.x);
-        const bool accB = actB && (s2 < 0.f || s2 < rhs.y);
-        const bool self = meta.w <= 1 && cm.w > 0.f;
-        const bool useA = accA && self && d2.x > 0.f, useB = accB && self && d2.y > 0.f;
+        bool accA, accB, useA, useB;
+        if (GUARD) {
+            accA = actA && (s2 < 0.f || s2 < rhs.x);
+            accB = actB && (s2 < 0.f || s2 < rhs.y);
+            const bool self = meta.w <= 1 && cm.w > 0.f;
+            useA = accA && self && d2.x > 0.f;
+            useB = accB && self && d2.y > 0.f;
+        } else {
+            accA = actA && s2 < rhs.x;
+            accB = actB && s2 < rhs.y;
+            const bool self = meta.w <= 1;  // a bucket's bodies are summed one by one below
+            useA = accA && self;
+            useB = accB && self;
+        }
         if (useA || useB) {
             if (COUNT) n_pairs += (useA ? 1u : 0u) + (useB ? 1u : 0u);
             const float2 e = make_float2(d2.x + eps2, d2.y + eps2);
@@ -862,10 +909,15 @@ __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict
         }
         if (meta.w != 0 && meta.w != 1) {  // warp-uniform: a bucket or a terminal cell
             const int cntb = meta.w >= 2 ? meta.w : -meta.w;
-            if ((meta.w >= 2 && accA) || (meta.w < 0 && actA && !accA))
-                direct_sum_range(pos, n, meta.z, cntb, meA, eps2, fAx, fAy, fAz, n_pairs, COUNT, phiA, POT);
-            if ((meta.w >= 2 && accB) || (meta.w < 0 && actB && !accB))
-                direct_sum_range(pos, n, meta.z, cntb, meB, eps2, fBx, fBy, fBz, n_pairs, COUNT, phiB, POT);
+            const bool doA = (meta.w >= 2 && accA) || (meta.w < 0 && actA && !accA);
+            const bool doB = (meta.w >= 2 && accB) || (meta.w < 0 && actB && !accB);
+            if (COUNT || POT) {
+                const float4 meA = make_float4(-nx.x, -ny.x, -nz.x, 0.f), meB = make_float4(-nx.y, -ny.y, -nz.y, 0.f);
+                if (doA) direct_sum_range(pos, n, meta.z, cntb, meA, eps2, fAx, fAy, fAz, n_pairs, COUNT, phiA, POT);
+                if (doB) direct_sum_range(pos, n, meta.z, cntb, meB, eps2, fBx, fBy, fBz, n_pairs, COUNT, phiB, POT);
+            } else if (doA || doB) {
+                direct_sum_range2(pos, n, meta.z, cntb, nx, ny, nz, eps2, doA, doB, fAx, fAy, fAz, fBx, fBy, fBz);
+            }
         }
         const bool doneA = accA || (actA && meta.w < 0), doneB = accB || (actB && meta.w < 0);
         if (doneA) skipA = meta.y;
@@ -888,6 +940,17 @@ __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict
             atomicAdd(&counters[1], n_visits);
         }
     }
+    if (SEG) {
+        const int4 ww = work[warp];
+        const float4 prm = params[ww.x];
+        dt = prm.x;
+        euler = prm.w != 0.f ? 1 : 0;
+        base = ww.y;
+        end = ww.w;
+    }
+    const int64_t bA = base + lane, bB = bA + 32;
+    vA = bA < end;
+    vB = bB < end;
     if (POT) {
         if (vA) {
             const int d = ids ? ids[bA] : static_cast<int>(bA);
@@ -899,8 +962,10 @@ __global__ void __launch_bounds__(256) traverse2_kernel(const BHNode *__restrict
         }
         return;
     }
-    if (vA) integrate_sorted(bA, meA, fAx, fAy, fAz, dt, pos_out, vel, acc, force_out, ids, n, euler);
-    if (vB) integrate_sorted(bB, meB, fBx, fBy, fBz, dt, pos_out, vel, acc, force_out, ids, n, euler);
+    // SEG reads the positions again (an L1/L2 hit) to keep registers free
+    // during the walk; the single-system walk keeps them.
+    if (vA) integrate_sorted(bA, SEG ? pos[bA] : meA0, fAx, fAy, fAz, dt, pos_out, vel, acc, force_out, ids, n, euler);
+    if (vB) integrate_sorted(bB, SEG ? pos[bB] : meB0, fBx, fBy, fBz, dt, pos_out, vel, acc, force_out, ids, n, euler);
 }
 
 // out[ids[i]] = in[i] (back to the caller's body order), positions with w = 0.
@@ -1158,11 +1223,15 @@ cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &
         const int64_t warps = (n + 63) / 64;
         const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
         if (w.counters)
-            traverse2_kernel<true, false, false><<<blocks, 256, 0, st>>>(
+            traverse2_kernel<true, false, false, true><<<blocks, 256, 0, st>>>(
                 w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, w.counters,
                 nullptr, euler, nullptr, 0, nullptr, nullptr);
+        else if (eps2 > 0.f && theta2 > 0.f)
+            traverse2_kernel<false, false, false, false><<<blocks, 256, 0, st>>>(
+                w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, nullptr,
+                nullptr, euler, nullptr, 0, nullptr, nullptr);
         else
-            traverse2_kernel<false, false, false><<<blocks, 256, 0, st>>>(
+            traverse2_kernel<false, false, false, true><<<blocks, 256, 0, st>>>(
                 w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, nullptr,
                 nullptr, euler, nullptr, 0, nullptr, nullptr);
     } else if (w.counters)
@@ -1179,7 +1248,7 @@ cudaError_t bh_potential(const float4 *pos_sorted, int64_t n, const BHWorkspace 
                          float *phi_out, const int *ids, cudaStream_t st) {
     const int64_t warps = (n + 63) / 64;
     const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
-    traverse2_kernel<false, true, false><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, 0.f,
+    traverse2_kernel<false, true, false, true><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, 0.f,
                                                                  nullptr, nullptr, nullptr, nullptr, ids, nullptr,
                                                                  phi_out, 0, nullptr, 0, nullptr, nullptr);
     return cudaGetLastError();
@@ -1240,13 +1309,17 @@ cudaError_t bh_ensemble_step(int64_t n, BHWorkspace &w, const BHEnsembleTables &
     if (tm) tm->begin(kStageTraverse, st);
     const unsigned blocks = static_cast<unsigned>((static_cast<int64_t>(e.nwarps) * 32 + 255) / 256);
     if (w.counters)
-        traverse2_kernel<true, false, true><<<blocks, 256, 0, st>>>(w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo,
-                                                                    Ao, nullptr, nullptr, w.counters, nullptr, 0,
-                                                                    e.warps, e.nwarps, e.params, w.P);
+        traverse2_kernel<true, false, true, true><<<blocks, 256, 0, st>>>(w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P,
+                                                                          Vo, Ao, nullptr, nullptr, w.counters,
+                                                                          nullptr, 0, e.warps, e.nwarps, e.params, w.P);
+    else if (e.all_soft)
+        traverse2_kernel<false, false, true, false><<<blocks, 256, 0, st>>>(
+            w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr, nullptr, nullptr, nullptr, 0, e.warps,
+            e.nwarps, e.params, w.P);
     else
-        traverse2_kernel<false, false, true><<<blocks, 256, 0, st>>>(w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo,
-                                                                     Ao, nullptr, nullptr, nullptr, nullptr, 0,
-                                                                     e.warps, e.nwarps, e.params, w.P);
+        traverse2_kernel<false, false, true, true><<<blocks, 256, 0, st>>>(
+            w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr, nullptr, nullptr, nullptr, 0, e.warps,
+            e.nwarps, e.params, w.P);
     if (tm) tm->end(kStageTraverse, st);
     return cudaGetLastError();
 }

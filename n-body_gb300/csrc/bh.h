@@ -107,6 +107,7 @@ struct BHEnsembleTables {
     float4 *params = nullptr;       // per system: dt, eps2, theta2, euler (0 / 1)
     uint64_t *keys_orig = nullptr;  // per body: unsorted key
     int seg_passes = 1;             // 8-bit digits of the system id
+    bool all_soft = false;          // every system has eps2 > 0 and theta2 > 0
 };
 
 // Host helper: the reference's fixed top-level depth for n bodies.

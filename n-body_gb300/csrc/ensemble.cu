@@ -364,6 +364,8 @@ int relayout(nbody_ensemble *e) {
         t.params = take<float4>(p, nsys);
         t.keys_orig = take<uint64_t>(p, static_cast<size_t>(bh_n));
         t.seg_passes = nsys <= 256 ? 1 : nsys <= 65536 ? 2 : 3;
+        t.all_soft = true;
+        for (int id : bh) t.all_soft = t.all_soft && e->sys[id].eps2 > 0.f && e->sys[id].theta2 > 0.f;
         EN_CK(e, cudaMemcpyAsync(t.seg, seg.data(), seg.size() * sizeof(int), cudaMemcpyHostToDevice, e->stream));
         EN_CK(e, cudaMemcpyAsync(t.chunks, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice,
                                  e->stream));
