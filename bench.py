@@ -23,6 +23,12 @@ no public dataset is involved):
        graphs. Metric: sims/s (a sim = one system for 50 steps), beside the
        same systems stepped one at a time by the single-system solver. The
        default line nests it as "ensemble".
+  serving: Poisson request streams (Plummer a = 100 or uniform ball R = 100,
+       N log-uniform in [1024, 4194304], steps U[10, 500], dt in {0.001,
+       0.0035}, eps^2 U[10, 40], theta = 0.5) served by the continuous-batching
+       loop under a 150 GB budget, beside FIFO one-at-a-time single-system
+       solves; p50 / p99 latency and sims/s. The default line nests one rate
+       (100 req/s, 12 requests) as "serving".
 
 A "step" is one ParticleSolver::updateParticlePositions: forces + integrator.
 value: K steps on HBM-resident state, timed with CUDA events on the launch
@@ -602,8 +608,8 @@ def bench_serving(args, world, rank, local, dist, rates=(10.0, 100.0, 1000.0), c
     per_rate = []
     for rate in rates:
         reqs = serving.poisson_trace(count, rate=rate, seed=11 + rank)
-        with serving.Server(budget_bytes=SERVE_BUDGET, device=local, crossover=X, pp_shape=shape,
-                            max_chunk=10) as srv:
+        with serving.LaneServer(budget_bytes=SERVE_BUDGET, device=local, crossover=X, pp_shape=shape,
+                                max_chunk=10) as srv:
             # warm-up request (module load, first allocations), untimed
             srv.run_trace([serving.Request(rid=-1, n=4096, steps=3, dt=0.001, eps2=10.0)], realtime=False)
             sampler = ClockSampler(local)
@@ -634,7 +640,7 @@ def bench_serving(args, world, rank, local, dist, rates=(10.0, 100.0, 1000.0), c
                                                               max(1e-12, s_sum["p99_latency_s"]), 3),
                          "max_in_flight": stats.max_in_flight, "chunks": stats.chunks,
                          "peak_footprint_gb": round(stats.peak_footprint / 1e9, 2),
-                         "gpu_busy_frac": round(stats.busy_seconds / max(1e-9, s_sum["makespan_s"]), 3),
+                         "policy": "4 priority lanes (ensembles on CUDA streams of decreasing priority by N x steps)",
                          "bh_requests_bit_equal_alone": f"{bh_equal}/{n_bh}",
                          "pp_requests_max_accel_rms_rel_vs_alone": pp_err, "clocks": clocks})
     head = max(per_rate, key=lambda d: d["rate_req_per_s"])
@@ -645,7 +651,7 @@ def bench_serving(args, world, rank, local, dist, rates=(10.0, 100.0, 1000.0), c
             "config": {"workload": f"serving: {count} requests per rate, Poisson arrivals; Plummer a=100 or uniform "
                                    f"ball R=100, N log-uniform in [1024, 4194304], steps U[10, 500], dt in "
                                    f"{{0.001, 0.0035}}, eps2 U[10, 40], theta=0.5; admission by HBM footprint under "
-                                   f"150 GB; continuous batching in chunks of <= 10 steps", "requests": count,
+                                   f"150 GB; continuous batching in chunks of <= 10 steps, in 4 priority lanes by N x steps", "requests": count,
                        "rates": list(rates), "crossover": X, "pp_shape": shape,
                        "body_steps_per_trace": int(body_steps), "parallelism": "replicas"},
             "p50_latency_s": head["served"]["p50_latency_s"], "p99_latency_s": head["served"]["p99_latency_s"],
@@ -799,6 +805,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-pp", action="store_true", help="leave the nested direct-sum measurement out")
     ap.add_argument("--no-ensemble", action="store_true", help="leave the nested ensemble measurement out")
+    ap.add_argument("--no-serving", action="store_true", help="leave the nested serving measurement out")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_env()
@@ -834,6 +841,11 @@ def main():
                                                    "e2e", "clocks", "gpu_launches", "config", "plain_loop",
                                                    "speedup_vs_plain", "body_steps_per_s", "cpu_baseline")
                                 if k in en}
+        if not args.no_serving and args.workload == "bh":
+            sv = bench_serving(args, world, rank, local, dist, rates=(100.0,), count=12)
+            line["serving"] = {k: sv[k] for k in ("component", "value", "unit", "p50_latency_s", "p99_latency_s",
+                                                  "plain_fifo", "speedup_vs_plain", "per_rate", "config", "e2e")
+                               if k in sv}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

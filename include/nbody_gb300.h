@@ -248,6 +248,8 @@ typedef struct nbody_ensemble nbody_ensemble;
 int nbody_ensemble_create(nbody_ensemble **out, int device, int64_t crossover);
 int nbody_ensemble_destroy(nbody_ensemble *e);
 const char *nbody_ensemble_last_error(const nbody_ensemble *e);
+/* Launches go to `stream` (NULL: the ensemble's own); the direct-sum side
+ * stream takes that stream's priority. */
 int nbody_ensemble_set_stream(nbody_ensemble *e, void *stream);
 /* pp_shape: direct-sum launch shape 0 = 128 threads x 2 bodies, 1 = 256 x 2
  * (default), 2 = 256 x 4; key_mode: NBODY_KEYS_*. */

@@ -541,9 +541,20 @@ const char *nbody_ensemble_last_error(const nbody_ensemble *e) { return e ? e->l
 int nbody_ensemble_set_stream(nbody_ensemble *e, void *stream) {
     if (!e) return NBODY_ERR_ARG;
     DevGuard dg(e->device);
-    // Work already queued on the old stream finishes first.
+    // Work already queued on the old streams finishes first.
     if (e->stream) EN_CK(e, cudaStreamSynchronize(e->stream));
+    if (e->side) EN_CK(e, cudaStreamSynchronize(e->side));
     e->stream = stream ? static_cast<cudaStream_t>(stream) : e->own_stream;
+    // The side stream (direct-sum launch) takes the caller's stream priority.
+    int prio = 0, side_prio = 0;
+    EN_CK(e, cudaStreamGetPriority(e->stream, &prio));
+    EN_CK(e, cudaStreamGetPriority(e->side, &side_prio));
+    if (prio != side_prio) {
+        cudaStream_t ns = nullptr;
+        EN_CK(e, cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, prio));
+        cudaStreamDestroy(e->side);
+        e->side = ns;
+    }
     clear_graphs(e);
     return NBODY_OK;
 }

@@ -81,6 +81,9 @@ def percentile(xs, q) -> float:
 
 
 class Server:
+    """Continuous batching in one shared ensemble: every admitted request steps
+    in every chunk (processor sharing)."""
+
     def __init__(self, budget_bytes: float = 150e9, device: int = 0, crossover: int | None = None,
                  pp_shape: str | None = None, max_chunk: int = 10, keep_results: bool = True, ensemble=None):
         """`ensemble` replaces the device ensemble (any object with the
@@ -205,6 +208,194 @@ class Server:
                 results[a.req.rid] = Result(a.req.rid, True, a.mode, system, arrival=a.req.arrival,
                                             admitted=a.admitted, completed=now())
             active = still
+        return results
+
+
+# Lane bounds in body-steps (N x steps) of a request's whole run.
+LANE_BOUNDS = (2e7, 2e8, 2e9)
+
+
+class _Lane:
+    def __init__(self, index, ens, stream):
+        self.index = index
+        self.ens = ens
+        self.stream = stream
+        self.active: list[_Active] = []
+        self.incoming: list[tuple] = []  # admitted (memory reserved), joins at the lane's next chunk
+        self.event = None  # set while a chunk is in flight
+        self.chunk = 0
+
+
+class LaneServer:
+    """Continuous batching in priority lanes. A request joins the lane of its
+    total work (N x steps; bounds LANE_BOUNDS), each lane is an ensemble on
+    its own CUDA stream, smaller work on higher stream priority. Every lane
+    with work has a chunk in flight, so lanes overlap on the GPU while the block
+    scheduler favours the small ones; finished chunks are noticed by polling
+    their events, their finished requests retired and arrivals admitted
+    (arrival order, shared memory budget). Results do not depend on lanes:
+    every system is computed on its own."""
+
+    def __init__(self, budget_bytes: float = 150e9, device: int = 0, crossover: int | None = None,
+                 pp_shape: str | None = None, max_chunk: int = 10, keep_results: bool = True,
+                 bounds=LANE_BOUNDS):
+        import torch
+
+        if crossover is None or pp_shape is None:
+            from .autotune import load_or_tune
+
+            t = load_or_tune(device)
+            crossover = t["crossover"] if crossover is None else crossover
+            pp_shape = t["pp_shape"] if pp_shape is None else pp_shape
+        self.budget = int(budget_bytes)
+        self.crossover = int(crossover)
+        self.pp_shape = pp_shape
+        self.device = device
+        self.max_chunk = int(max_chunk)
+        self.keep_results = keep_results
+        self.bounds = tuple(bounds)
+        self.stats = ServerStats()
+        lo, hi = torch.cuda.Stream.priority_range()  # e.g. (0, -5): lower is more urgent
+        nl = len(self.bounds) + 1
+        self.lanes = []
+        for k in range(nl):
+            prio = hi + round((lo - hi) * k / max(1, nl - 1)) if lo != hi else lo
+            stream = torch.cuda.Stream(device=device, priority=int(prio))
+            ens = Ensemble(crossover=self.crossover, device=device, pp_shape=pp_shape)
+            ens.set_stream(stream.cuda_stream)
+            self.lanes.append(_Lane(k, ens, stream))
+
+    def close(self) -> None:
+        for lane in self.lanes:
+            lane.ens.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def footprint(self, req: Request) -> int:
+        mode = "pp" if req.n < self.crossover else "bh"
+        return 2 * Ensemble.footprint(req.n, mode)
+
+    def lane_of(self, req: Request) -> int:
+        work = float(req.n) * req.steps
+        for k, b in enumerate(self.bounds):
+            if work < b:
+                return k
+        return len(self.bounds)
+
+    def run_trace(self, requests, realtime: bool = True, clock=time.perf_counter):
+        import torch
+
+        pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
+        queue: list[Request] = []
+        results: dict[int, Result] = {}
+        used = 0
+        t0 = clock()
+        now = lambda: clock() - t0  # noqa: E731
+        st = self.stats
+
+        def fail(a, lane, err):
+            results[a.req.rid] = Result(a.req.rid, False, a.mode, error=err, arrival=a.req.arrival,
+                                        admitted=a.admitted, completed=now())
+            lane.ens.remove(a.sid)
+
+        while pending or queue or any(l.active or l.incoming for l in self.lanes):
+            t = now()
+            while pending and (not realtime or pending[0].arrival <= t):
+                queue.append(pending.pop(0))
+            # retire lanes whose chunk has finished
+            for lane in self.lanes:
+                if lane.event is None or not lane.event.query():
+                    continue
+                lane.event = None
+                k = lane.chunk
+                try:
+                    lane.ens.sync()
+                except NBodyError as e:
+                    for a in lane.active:
+                        fail(a, lane, str(e))
+                        used -= a.footprint
+                    lane.active = []
+                    continue
+                still = []
+                for a in lane.active:
+                    a.left -= k
+                    if a.left > 0:
+                        still.append(a)
+                        continue
+                    system = lane.ens.download(a.sid) if self.keep_results else None
+                    lane.ens.remove(a.sid)
+                    used -= a.footprint
+                    results[a.req.rid] = Result(a.req.rid, True, a.mode, system, arrival=a.req.arrival,
+                                                admitted=a.admitted, completed=now())
+                lane.active = still
+            # admission in arrival order under the shared memory budget; the
+            # request joins its lane's ensemble when the lane is idle
+            while queue:
+                req = queue[0]
+                fp = self.footprint(req)
+                if fp > self.budget:
+                    queue.pop(0)
+                    results[req.rid] = Result(req.rid, False, error="larger than the memory budget",
+                                              arrival=req.arrival, admitted=now(), completed=now())
+                    continue
+                if used + fp > self.budget:
+                    break
+                queue.pop(0)
+                self.lanes[self.lane_of(req)].incoming.append((req, fp, now()))
+                used += fp
+            # an idle lane takes its incoming requests, then every idle lane with
+            # work launches a chunk
+            launched = False
+            for lane in self.lanes:
+                if lane.event is not None:
+                    continue
+                ens = lane.ens
+                for req, fp, t_adm in lane.incoming:
+                    try:
+                        sid = ens.add(req.n, req.dt, req.eps2, req.theta2)
+                        try:
+                            if req.init == "state":
+                                if req.state is None or req.state.n != req.n:
+                                    raise ValueError("request state missing or of the wrong size")
+                                ens.upload(sid, req.state)
+                            else:
+                                ens.init_device(sid, req.init, seed=req.seed, params=req.params)
+                        except Exception:
+                            ens.remove(sid)
+                            raise
+                    except (NBodyError, ValueError) as e:
+                        results[req.rid] = Result(req.rid, False, error=str(e), arrival=req.arrival,
+                                                  admitted=t_adm, completed=now())
+                        used -= fp
+                        continue
+                    lane.active.append(_Active(req, sid, req.steps, fp, t_adm, ens.info(sid)[0]))
+                lane.incoming = []
+                if not lane.active:
+                    continue
+                k = min(self.max_chunk, min(a.left for a in lane.active))
+                try:
+                    lane.ens.step(k)
+                except NBodyError as e:
+                    for a in lane.active:
+                        fail(a, lane, str(e))
+                        used -= a.footprint
+                    lane.active = []
+                    continue
+                ev = torch.cuda.Event()
+                ev.record(lane.stream)
+                lane.event, lane.chunk = ev, k
+                st.chunks += 1
+                st.steps += k
+                launched = True
+            in_flight = sum(len(l.active) for l in self.lanes)
+            st.max_in_flight = max(st.max_in_flight, in_flight)
+            st.peak_footprint = max(st.peak_footprint, used)
+            if not launched:
+                time.sleep(0.0002)
         return results
 
 

@@ -57,6 +57,25 @@ def test_served_results_equal_each_request_alone(nb, cuda):
         _same(one[r.rid].system, res[r.rid].system)
 
 
+def test_lane_server_results_equal_each_request_alone(nb, cuda):
+    """Priority lanes (concurrent ensembles on streams of different priority)
+    give the same bits as the shared server, request by request."""
+    from nbody_gb300 import serving
+
+    reqs = _trace(serving)
+    with serving.Server(budget_bytes=1e10, crossover=4096, pp_shape="128x2", max_chunk=3) as srv:
+        shared = srv.run_trace(reqs, realtime=False)
+    # bounds that spread this small trace over all four lanes
+    with serving.LaneServer(budget_bytes=1e10, crossover=4096, pp_shape="128x2", max_chunk=3,
+                            bounds=(2e4, 1e5, 2e5)) as srv:
+        lanes = srv.run_trace(reqs, realtime=True)
+        used = {srv.lane_of(r) for r in reqs}
+        assert len(used) >= 3
+    for r in reqs:
+        assert lanes[r.rid].ok, lanes[r.rid].error
+        _same(lanes[r.rid].system, shared[r.rid].system)
+
+
 def test_requests_with_explicit_states(nb, cuda):
     from nbody_gb300 import initializers as I
     from nbody_gb300 import serving
