@@ -187,6 +187,20 @@ def barrier(dist):
         dist.barrier()
 
 
+def profile_value(kernel: str, key: str):
+    """A number `key: value` from a committed ncu summary (profiles/<kernel>*.md), if any."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for fn in sorted(os.listdir(pdir)):
+        if fn.startswith(kernel) and fn.endswith(".md"):
+            with open(os.path.join(pdir, fn)) as f:
+                m = re.search(key + r":\s*([0-9.eE+]+)", f.read())
+            if m:
+                return float(m.group(1))
+    return None
+
+
 def profile_traffic(kernel: str):
     """DRAM bytes per launch from a committed ncu summary (profiles/<kernel>*.md), if any."""
     pdir = os.path.join(ROOT, "profiles")
@@ -510,8 +524,13 @@ def bench_ensemble(args, world, rank, local, dist, steps=None):
     pp_pairs = float(np.sum(pp_sizes.astype(np.float64) ** 2))
     pp_tf = FLOP_PER_INTERACTION * pp_pairs / pp_launch / 1e12 if pp_launch > 0 else 0.0
     bh_ms = sum(v[0] / max(1, v[1]) for k_, v in prof.items() if k_.startswith("bh_"))
+    per_body = profile_value("pp_batch_kernel", "traffic_bytes_per_body")
     roofline = {"bound": "fp32", "achieved": round(pp_tf, 3), "peak": round(fp32, 3), "unit": "TFLOP/s",
-                "frac": round(pp_tf / fp32, 4), "traffic": None, "kernel": "pp_batch_kernel",
+                "frac": round(pp_tf / fp32, 4),
+                "traffic": round(per_body * float(pp_sizes.sum())) if per_body else None,
+                "traffic_note": "DRAM bytes per body of a smaller capture (profiles/pp_batch_kernel_ensemble_256_"
+                                "systems.md) times this launch's direct-sum bodies",
+                "kernel": "pp_batch_kernel",
                 "kernel_ms_per_launch": round(pp_launch * 1e3, 4),
                 "note": "the batched direct-sum kernel over the systems below the crossover (sum of N^2 pairs, "
                         "20 flop each); the Barnes-Hut stages of the other systems run beside it",
