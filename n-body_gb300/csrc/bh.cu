@@ -823,7 +823,7 @@ __device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, 
 // theta2 * d2 >= 0, and a record at zero distance adds dx * w = +0 to every
 // component, so the accepted set and the sums are the same bit for bit.
 template <bool COUNT, bool POT, bool SEG, bool GUARD>
-__global__ void __launch_bounds__(256, SEG ? 5 : 6) traverse2_kernel(const BHNode *__restrict__ nodes,
+__global__ void __launch_bounds__(256, SEG ? 5 : (POT ? 1 : 6)) traverse2_kernel(const BHNode *__restrict__ nodes,
                                                         const uint32_t *__restrict__ node_total,
                                                         const float4 *__restrict__ pos, int64_t n, float eps2,
                                                         float theta2, float dt, float4 *__restrict__ pos_out,

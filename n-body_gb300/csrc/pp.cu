@@ -33,8 +33,17 @@ namespace nbody {
 
 constexpr int kPPMinThreads = 128;
 
+// Launch bounds: K <= 2 takes the compiler's register choice (64 registers,
+// 4 CTAs of 256 per SM); K >= 4 allows up to 255 registers per thread so that
+// all K i-bodies' accumulators and the unrolled j-pairs stay in registers:
+// fewer warps, more independent FMA chains per thread.
+template <int K>
+constexpr int pp_min_blocks() {
+    return K >= 4 ? 1 : 0;
+}
+
 template <int K, int T, bool GUARD>
-__global__ void __launch_bounds__(T)
+__global__ void __launch_bounds__(T, pp_min_blocks<K>())
     pp_force_kernel(const float4 *__restrict__ pos, int64_t n, float eps2, int nslices,
                     float4 *__restrict__ partial, unsigned *__restrict__ arrivals, Integrate g, int *status) {
     // tile: TMA landing zone, bodies as float4 (x, y, z, m).
