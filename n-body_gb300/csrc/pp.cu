@@ -290,9 +290,11 @@ int k_index(int k) { return k == 1 ? 0 : k == 2 ? 1 : k == 4 ? 2 : 3; }
 PPPlan pp_plan(int64_t n, int device) {
     PPPlan p;
     const DeviceInfo d = device_info(device);
-    // Default shape from a sweep at N = 16,384 on GB300 (T x K in {128, 256} x
-    // {1, 2, 4, 8}): 256 threads with 2 i-bodies each was fastest.
-    int k = 2;
+    // Default shapes from sweeps on GB300 (T x K in {128, 256} x {1, 2, 4, 8},
+    // N = 4,096 ... 131,072): from N = 8,192 on, 256 threads with 4 i-bodies
+    // each (one CTA per SM at 140 registers, ILP-bound) is fastest; below it 2
+    // i-bodies per thread give the j-slicing enough CTAs.
+    int k = n >= 8192 ? 4 : 2;
     if (const char *e = std::getenv("NBODY_PP_K")) {
         const int v = std::atoi(e);
         if (v == 1 || v == 2 || v == 4 || v == 8) k = v;
