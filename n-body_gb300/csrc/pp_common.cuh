@@ -50,4 +50,90 @@ __device__ __forceinline__ void integrate_body(int64_t i, float4 p, float fx, fl
     if (g.force) g.force[i] = anew;
 }
 
+// Shared-memory staging of one CTA: the TMA landing ring and the j-pair tile.
+struct Ring {
+    float4 (*tile)[kPPTile];
+    float4 *pairs;
+    uint64_t *full;
+};
+
+// Accumulates the forces on this thread's K i-bodies from bodies [j0, j1),
+// through the TMA ring; `gt` counts the tiles this CTA has consumed (ring
+// position and mbarrier phase). Returns false if a copy never landed.
+template <int K, int T, bool GUARD>
+__device__ bool item_forces(const float4 *__restrict__ pos, int64_t j0, int64_t j1, const float2 (&nx)[K],
+                            const float2 (&ny)[K], const float2 (&nz)[K], float2 (&ax)[K], float2 (&ay)[K],
+                            float2 (&az)[K], float eps2, Ring ring, uint32_t &gt, int *status) {
+    const int tid = threadIdx.x;
+    const int64_t len = j1 - j0;
+    const int ntiles = static_cast<int>((len + kPPTile - 1) / kPPTile);
+    auto issue = [&](int t) {
+        const uint32_t g = gt + static_cast<uint32_t>(t);
+        const int stage = static_cast<int>(g % kPPStages);
+        const int64_t jt = j0 + static_cast<int64_t>(t) * kPPTile;
+        const int cnt = static_cast<int>((j1 - jt) < kPPTile ? (j1 - jt) : kPPTile);
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&ring.full[stage], static_cast<uint32_t>(cnt) * 16u);
+        tma_bulk_g2s(&ring.tile[stage][0], pos + jt, static_cast<uint32_t>(cnt) * 16u, &ring.full[stage]);
+    };
+    if (tid == 0)
+        for (int t = 0; t < kPPStages && t < ntiles; ++t) issue(t);
+    const float2 e2 = f2(eps2, eps2);
+    for (int t = 0; t < ntiles; ++t) {
+        const uint32_t g = gt + static_cast<uint32_t>(t);
+        const int stage = static_cast<int>(g % kPPStages);
+        const uint32_t parity = (g / kPPStages) & 1u;
+        const bool ok = mbar_wait_bounded(&ring.full[stage], parity, status);
+        if (!__syncthreads_and(ok)) {
+            // Drain the copies still in flight before shared memory goes away.
+            if (tid == 0)
+                for (int u = t; u < ntiles && u < t + kPPStages; ++u) {
+                    const uint32_t gu = gt + static_cast<uint32_t>(u);
+                    mbar_wait_bounded(&ring.full[gu % kPPStages], (gu / kPPStages) & 1u, status);
+                }
+            __syncthreads();
+            return false;
+        }
+        const int64_t jt = j0 + static_cast<int64_t>(t) * kPPTile;
+        const int cnt = static_cast<int>((j1 - jt) < kPPTile ? (j1 - jt) : kPPTile);
+        const int npr = (cnt + 1) >> 1;
+        for (int q = tid; q < npr; q += T) {
+            const float4 a = ring.tile[stage][2 * q];
+            const float4 b = (2 * q + 1 < cnt) ? ring.tile[stage][2 * q + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+            ring.pairs[2 * q] = make_float4(a.x, b.x, a.y, b.y);
+            ring.pairs[2 * q + 1] = make_float4(a.z, b.z, a.w, b.w);
+        }
+        __syncthreads();
+        if (tid == 0 && t + kPPStages < ntiles) issue(t + kPPStages);
+        const float4 *pr = ring.pairs;
+#pragma unroll 2
+        for (int q = 0; q < npr; ++q) {
+            const float4 u = pr[2 * q];
+            const float4 v = pr[2 * q + 1];
+            const float2 xj = f2(u.x, u.y), yj = f2(u.z, u.w), zj = f2(v.x, v.y), mj = f2(v.z, v.w);
+#pragma unroll
+            for (int r = 0; r < K; ++r) {
+                const float2 dx = __fadd2_rn(xj, nx[r]);
+                const float2 dy = __fadd2_rn(yj, ny[r]);
+                const float2 dz = __fadd2_rn(zj, nz[r]);
+                float2 r2 = __ffma2_rn(dx, dx, e2);
+                r2 = __ffma2_rn(dy, dy, r2);
+                r2 = __ffma2_rn(dz, dz, r2);
+                float2 inv = f2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+                if (GUARD) {
+                    inv.x = r2.x > 0.f ? inv.x : 0.f;
+                    inv.y = r2.y > 0.f ? inv.y : 0.f;
+                }
+                const float2 inv2 = __fmul2_rn(inv, inv);
+                const float2 s = __fmul2_rn(__fmul2_rn(mj, inv), inv2);
+                ax[r] = __ffma2_rn(dx, s, ax[r]);
+                ay[r] = __ffma2_rn(dy, s, ay[r]);
+                az[r] = __ffma2_rn(dz, s, az[r]);
+            }
+        }
+    }
+    gt += static_cast<uint32_t>(ntiles);
+    return true;
+}
+
 }  // namespace nbody
