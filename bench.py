@@ -444,8 +444,8 @@ def bench_bh(args, world, rank, local, dist):
                                     "(reference -v 6 path)"), "n_bodies": n, "parallelism": "replicas",
                        "l2": "flushed between steps (256 MiB write, outside the event pair)"},
             "clocks": clocks, "roofline": roofline, "e2e": e2e, "gpu_launches": launches_per_step * args.steps}
-    if rank == 0 and not args.no_cpu_baseline and not discs:
-        line["cpu_baseline"] = cpu_baseline_bh()
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_discs(pos, vel, mass) if discs else cpu_baseline_bh()
     solver.close()
     torch.cuda.set_stream(torch.cuda.default_stream())
     return line
@@ -709,6 +709,43 @@ def cpu_baseline_ensemble(sizes, crossover, sample: int = 24, seed: int = 3):
                       f"threads), scaled to 2048 systems x 50 steps"}
 
 
+def cpu_baseline_serving(count: int, sample: int = 6, seed: int = 11):
+    """The port serving a random sample of the trace's requests (one step each, scaled by their step counts),
+    scaled to the whole trace: requests per second of FIFO service on the host cores."""
+    import pyoracle
+    from nbody_gb300 import initializers as I
+    from nbody_gb300 import serving
+
+    pyoracle.build(reference=False)
+    threads = cpu_threads()
+    from nbody_gb300 import autotune
+
+    with open(autotune.default_path("NVIDIA GB300")) as f:
+        crossover = int(json.load(f)["crossover"])
+    reqs = serving.poisson_trace(count, rate=100.0, seed=seed)
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(len(reqs), size=min(sample, len(reqs)), replace=False)
+    secs = 0.0
+    for j in pick:
+        r = reqs[int(j)]
+        if r.init == "plummer":
+            pos, vel, mass = I.plummer(r.n, a=100.0, seed=int(j))
+        else:
+            pos, vel, mass = I.uniform_ball(r.n, radius=100.0, seed=int(j))
+        acc = np.zeros_like(pos)
+        if r.n < crossover:  # the same method as the served arm: direct sum below the crossover
+            one = pyoracle.pp_run(pos, vel, acc, mass, r.dt, r.eps2, 1, threads=threads)[4]
+        else:
+            one = pyoracle.bh_run(pos, vel, acc, mass, r.dt, r.eps2, 1, theta2=r.theta2, threads=threads,
+                                  patched=True)[4]["seconds"]
+        secs += one * r.steps
+    total = secs * len(reqs) / len(pick)
+    return {"value": len(reqs) / total, "unit": "sims/s", "cores": threads, "kind": "port",
+            "sample": f"one step (restated -v 2 below the crossover, -v 6 above, {threads} threads) of each of "
+                      f"{len(pick)} randomly chosen requests, times its step count, scaled to the {len(reqs)}-request "
+                      f"trace"}
+
+
 def cpu_baseline_bh(budget_s: float = 15.0):
     import pyoracle
     from nbody_gb300 import initializers as I
@@ -726,6 +763,19 @@ def cpu_baseline_bh(budget_s: float = 15.0):
                                       f"OpenMP tasks, integer node links, subtree regions sized from their "
                                       f"body counts; the reference's own -v 6 overflows its fixed regions on "
                                       f"this input), {threads} threads"}
+
+
+def cpu_baseline_discs(pos, vel, mass):
+    """One full -v 6 step (restated port) of the 16,777,216-body discs workload on the host cores."""
+    import pyoracle
+
+    pyoracle.build(reference=False)
+    threads = cpu_threads()
+    acc = np.zeros_like(pos)
+    r = pyoracle.bh_run(pos, vel, acc, mass, BH_DT, BH_EPS2, 1, theta2=DISCS_THETA2, threads=threads, patched=True)
+    return {"value": float(len(mass)) / r[4]["seconds"], "unit": "body-steps/s", "cores": threads, "kind": "port",
+            "sample": f"1 full step of the N=16777216 discs workload (-v 6 restated: OpenMP tasks, integer node "
+                      f"links, subtree regions sized from their body counts), theta=0.6, {threads} threads"}
 
 
 def cpu_kind():
@@ -785,6 +835,43 @@ def bench_reference(args, world, rank):
                     "(reference -v 2 path)")
         sample = f"{steps} full steps (-v 2 OpenMP, {threads} threads)"
         n = PP_N
+    elif args.workload in ("ensemble", "serving"):
+        if args.workload == "ensemble":
+            from nbody_gb300 import autotune
+
+            tune_path = autotune.default_path("NVIDIA GB300")
+            with open(tune_path) as f:
+                X = int(json.load(f)["crossover"])
+            sizes = I.ragged_sizes(ENS_COUNT, ENS_LO, ENS_HI, seed=2024)
+            cb = cpu_baseline_ensemble(sizes, X)
+            workload = ("batched ragged ensemble: 2048 Plummer clusters (a=50, m=1), N log-uniform in [256, 131072]; "
+                        "direct sum below the crossover, Barnes-Hut theta=0.5 above; a sim = one system for 50 steps")
+            n = int(sizes.sum())
+        else:
+            cb = cpu_baseline_serving(args.requests)
+            workload = ("serving trace: Plummer a=100 or uniform ball R=100, N log-uniform in [1024, 4194304], steps "
+                        "U[10, 500]; requests served one at a time on the host cores")
+            n = None
+        value, unit, kind, sample = cb["value"], cb["unit"], cb["kind"], cb["sample"]
+        comp, steps, secs = ("batched ensemble sims/s" if args.workload == "ensemble" else "served sims/s"), 1, 1.0
+    elif args.workload == "discs":
+        pos, vel, mass = I.two_discs(seed=12345)
+        acc = np.zeros_like(pos)
+        # one warm-up step, then at most two timed full -v 6 steps (each ~30 s)
+        pyoracle.bh_run(pos, vel, acc, mass, BH_DT, BH_EPS2, 1, theta2=DISCS_THETA2, threads=threads, patched=True)
+        steps = max(1, min(args.steps, 2))
+        r = pyoracle.bh_run(pos, vel, acc, mass, BH_DT, BH_EPS2, steps, theta2=DISCS_THETA2, threads=threads,
+                            patched=True)
+        secs = r[4]["seconds"]
+        n = len(mass)
+        value = float(n) * steps / secs
+        kind = "port"
+        unit, comp = "body-steps/s", "BH body-steps/s"
+        workload = ("Barnes-Hut at scale, N=16777216: two exponential discs of 8388607 bodies (m=1, scale length "
+                    "200, sech^2 height 20, circular velocities) + a 1e6 point mass each, 2000 apart, relative speed "
+                    "50, inclined 30 deg; theta=0.6, eps2=40, dt=0.0035 (reference -v 6 path)")
+        sample = (f"{steps} full steps after 1 warm-up step (-v 6 restated with integer node links and subtree "
+                  f"regions sized from their body counts), {threads} threads")
     else:
         pos, vel, mass = I.plummer(BH_N, a=100.0, seed=12345)
         acc = np.zeros_like(pos)
@@ -805,8 +892,9 @@ def bench_reference(args, world, rank):
                   f"their body counts; the reference's own -v 6 overflows its fixed regions on this input), "
                   f"{threads} threads")
         n = BH_N
+    per_step = None if args.workload in ("ensemble", "serving") else secs * 1e3 / steps
     return {"impl": "reference", "metric": METRIC, "component": comp, "value": value, "unit": unit,
-            "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / steps,
+            "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload, "n_bodies": n, "parallelism": "host cores"},
             "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": kind, "sample": sample},
