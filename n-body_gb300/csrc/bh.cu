@@ -625,11 +625,9 @@ __global__ void upsweep_kernel(const uint64_t *__restrict__ k, int64_t n, const 
 // or a pair it skips (m == 0 or r^2 == 0), adds dx * 0 = +0 to its sums.
 __device__ __forceinline__ void direct_sum_range2(const float4 *__restrict__ pos, int64_t n, int first, int count,
                                                   float2 nx, float2 ny, float2 nz, float eps2, bool doA, bool doB,
-                                                  float &fAx, float &fAy, float &fAz, float &fBx, float &fBy,
-                                                  float &fBz) {
+                                                  float2 &ax, float2 &ay, float2 &az) {
     const int q0 = first < 0 ? 0 : first;
     const int q1 = first + count < n ? first + count : static_cast<int>(n);
-    float2 ax = make_float2(fAx, fBx), ay = make_float2(fAy, fBy), az = make_float2(fAz, fBz);
     for (int q = q0; q < q1; ++q) {
         const float4 o = pos[q];
         const float2 ex = __fadd2_rn(make_float2(o.x, o.x), nx);
@@ -644,12 +642,6 @@ __device__ __forceinline__ void direct_sum_range2(const float4 *__restrict__ pos
         ay = __ffma2_rn(ey, ws, ay);
         az = __ffma2_rn(ez, ws, az);
     }
-    fAx = ax.x;
-    fAy = ay.x;
-    fAz = az.x;
-    fBx = ax.y;
-    fBy = ay.y;
-    fBz = az.y;
 }
 
 __device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, float fy, float fz, float dt,
@@ -865,7 +857,10 @@ __global__ void __launch_bounds__(256, SEG ? 5 : (POT ? 1 : 6)) traverse2_kernel
                  nz = make_float2(-meA0.z, -meB0.z);
     const float2 th = make_float2(theta2, theta2);
     int skipA = vA ? i : m_nodes, skipB = vB ? i : m_nodes;
-    float fAx = 0.f, fAy = 0.f, fAz = 0.f, fBx = 0.f, fBy = 0.f, fBz = 0.f;
+    // Force sums of the lane's two bodies as packed pairs (x: body A, y: body B);
+    // an FFMA2 rounds each half exactly as a scalar FFMA.
+    float2 fx = make_float2(0.f, 0.f), fy = make_float2(0.f, 0.f), fz = make_float2(0.f, 0.f);
+    const float2 e2 = make_float2(eps2, eps2);
     while (i < m_nodes) {
         const float4 cm = __ldg(&nodes[i].cm);
         const int4 meta = __ldg(&nodes[i].meta);
@@ -892,16 +887,14 @@ __global__ void __launch_bounds__(256, SEG ? 5 : (POT ? 1 : 6)) traverse2_kernel
         }
         if (useA || useB) {
             if (COUNT) n_pairs += (useA ? 1u : 0u) + (useB ? 1u : 0u);
-            const float2 e = make_float2(d2.x + eps2, d2.y + eps2);
+            const float2 e = __fadd2_rn(d2, e2);
             const float2 inv = make_float2(rsqrt_ftz(e.x), rsqrt_ftz(e.y));
             const float2 inv3 = __fmul2_rn(__fmul2_rn(inv, inv), inv);
-            const float2 w = make_float2(useA ? cm.w * inv3.x : 0.f, useB ? cm.w * inv3.y : 0.f);
-            fAx = fmaf(dx.x, w.x, fAx);
-            fAy = fmaf(dy.x, w.x, fAy);
-            fAz = fmaf(dz.x, w.x, fAz);
-            fBx = fmaf(dx.y, w.y, fBx);
-            fBy = fmaf(dy.y, w.y, fBy);
-            fBz = fmaf(dz.y, w.y, fBz);
+            const float2 mw = __fmul2_rn(make_float2(cm.w, cm.w), inv3);
+            const float2 w = make_float2(useA ? mw.x : 0.f, useB ? mw.y : 0.f);
+            fx = __ffma2_rn(dx, w, fx);
+            fy = __ffma2_rn(dy, w, fy);
+            fz = __ffma2_rn(dz, w, fz);
             if (POT) {
                 phiA = fmaf(useA ? -cm.w : 0.f, inv.x, phiA);
                 phiB = fmaf(useB ? -cm.w : 0.f, inv.y, phiB);
@@ -913,10 +906,10 @@ __global__ void __launch_bounds__(256, SEG ? 5 : (POT ? 1 : 6)) traverse2_kernel
             const bool doB = (meta.w >= 2 && accB) || (meta.w < 0 && actB && !accB);
             if (COUNT || POT) {
                 const float4 meA = make_float4(-nx.x, -ny.x, -nz.x, 0.f), meB = make_float4(-nx.y, -ny.y, -nz.y, 0.f);
-                if (doA) direct_sum_range(pos, n, meta.z, cntb, meA, eps2, fAx, fAy, fAz, n_pairs, COUNT, phiA, POT);
-                if (doB) direct_sum_range(pos, n, meta.z, cntb, meB, eps2, fBx, fBy, fBz, n_pairs, COUNT, phiB, POT);
+                if (doA) direct_sum_range(pos, n, meta.z, cntb, meA, eps2, fx.x, fy.x, fz.x, n_pairs, COUNT, phiA, POT);
+                if (doB) direct_sum_range(pos, n, meta.z, cntb, meB, eps2, fx.y, fy.y, fz.y, n_pairs, COUNT, phiB, POT);
             } else if (doA || doB) {
-                direct_sum_range2(pos, n, meta.z, cntb, nx, ny, nz, eps2, doA, doB, fAx, fAy, fAz, fBx, fBy, fBz);
+                direct_sum_range2(pos, n, meta.z, cntb, nx, ny, nz, eps2, doA, doB, fx, fy, fz);
             }
         }
         const bool doneA = accA || (actA && meta.w < 0), doneB = accB || (actB && meta.w < 0);
@@ -964,8 +957,8 @@ __global__ void __launch_bounds__(256, SEG ? 5 : (POT ? 1 : 6)) traverse2_kernel
     }
     // SEG reads the positions again (an L1/L2 hit) to keep registers free
     // during the walk; the single-system walk keeps them.
-    if (vA) integrate_sorted(bA, SEG ? pos[bA] : meA0, fAx, fAy, fAz, dt, pos_out, vel, acc, force_out, ids, n, euler);
-    if (vB) integrate_sorted(bB, SEG ? pos[bB] : meB0, fBx, fBy, fBz, dt, pos_out, vel, acc, force_out, ids, n, euler);
+    if (vA) integrate_sorted(bA, SEG ? pos[bA] : meA0, fx.x, fy.x, fz.x, dt, pos_out, vel, acc, force_out, ids, n, euler);
+    if (vB) integrate_sorted(bB, SEG ? pos[bB] : meB0, fx.y, fy.y, fz.y, dt, pos_out, vel, acc, force_out, ids, n, euler);
 }
 
 // out[ids[i]] = in[i] (back to the caller's body order), positions with w = 0.
