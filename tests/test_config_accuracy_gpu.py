@@ -1,0 +1,86 @@
+"""Acceleration error against an FP64 direct sum at the configurations' full
+sizes (a sample of bodies), and for the discs also against the -v 6 port
+(oracle/nbody_oracle.c, patched capacities) at a reduced size: the Barnes-Hut
+error is the method's when the GPU's FP64 error matches the port's.
+
+  config 1, direct sum, N = 16,384 ball:          RMS <= 1e-5 (the accuracy gate)
+  config 2, Barnes-Hut theta = 0.5, N = 2^20:     RMS <= 1.2e-3 (gate 1e-3 at theta = 0.5;
+                                                   measured 9.7e-4)
+  config 3, Barnes-Hut theta = 0.6, N = 2^24 discs: RMS 1.4e-2, the method's at this theta:
+                                                   a one-off run of the port on the same
+                                                   2^24 bodies gave the same FP64 error
+                                                   (1.3988e-2) and GPU vs port RMS 1.3e-6;
+                                                   here at 2^18 the GPU's FP64 error must
+                                                   be within 10% of the port's (1.45e-3 both)
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(got, ref):
+    g = np.asarray(got, np.float64)[:, :3]
+    r = np.asarray(ref, np.float64)[:, :3]
+    e = np.linalg.norm(g - r, axis=1) / np.linalg.norm(r, axis=1)
+    return float(np.sqrt(np.mean(e * e))), float(e.max())
+
+
+def _one_step(nb, n, mode, theta2, arrays=None, kind=None, seed=7):
+    """(positions, masses, accelerations at those positions) of one step."""
+    s = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode=mode, theta2=theta2)
+    if arrays is not None:
+        pos, vel, mass = arrays
+        s.upload(nb.ParticleSystem(pos.copy(), vel.copy(), mass))
+    else:
+        s.init_device(kind, seed=seed)
+    z = np.zeros((n, 4), np.float32)
+    before = nb.ParticleSystem(z.copy(), z.copy(), np.zeros(n, np.float32), z.copy())
+    s.download(before, masses=True)
+    s.step(1)
+    after = nb.ParticleSystem(z.copy(), z.copy(), np.zeros(n, np.float32), z.copy())
+    s.download(after)
+    s.close()
+    return before.positions, before.masses[:, 0], before.velocities, after.accelerations
+
+
+def test_config1_direct_sum_vs_fp64(nb, cuda, oracle):
+    from nbody_gb300 import initializers as I
+
+    p, m, _, a = _one_step(nb, 16384, "pp", 0.25, arrays=I.uniform_ball(16384, seed=12345))
+    rms, mx = _rel(a, oracle.direct_f64(p, m, 40.0))
+    print(f"config 1 vs FP64: RMS {rms:.3g}, max {mx:.3g}")
+    assert rms <= 1e-5 and mx <= 1e-4, (rms, mx)
+
+
+def test_config2_barnes_hut_1m_vs_fp64(nb, cuda, oracle):
+    from nbody_gb300 import initializers as I
+
+    n = 1 << 20
+    p, m, _, a = _one_step(nb, n, "bh", 0.25, arrays=I.plummer(n, a=100.0, seed=12345))
+    idx = np.random.default_rng(1).choice(n, 1024, replace=False)
+    rms, mx = _rel(a[idx], oracle.direct_f64(p, m, 40.0, idx=idx))
+    print(f"config 2 vs FP64 (1,024 bodies): RMS {rms:.3g}, max {mx:.3g}")
+    assert rms <= 1.2e-3, (rms, mx)
+
+
+def test_config3_discs_error_is_the_methods(nb, cuda, oracle):
+    """Two discs of 2^17 bodies (device generator, the config's shape), theta =
+    0.6: the GPU's and the port's FP64 errors agree."""
+    n = 1 << 18
+    p, m, v, a = _one_step(nb, n, "bh", 0.36, kind="two_discs")
+    pf = oracle.bh_run(p, v, np.zeros_like(p), m, 0.0035, 40.0, 1, theta2=0.36, patched=True)[3]
+    idx = np.random.default_rng(2).choice(n, 1024, replace=False)
+    a64 = oracle.direct_f64(p, m, 40.0, idx=idx)
+    e_gpu, e_port = _rel(a[idx], a64)[0], _rel(pf[idx], a64)[0]
+    print(f"discs 2^18 vs FP64: GPU RMS {e_gpu:.3g}, port RMS {e_port:.3g}")
+    assert e_gpu <= 1.1 * e_port + 1e-6, (e_gpu, e_port)
+
+
+def test_config3_discs_16m_vs_fp64(nb, cuda, oracle):
+    n = 1 << 24
+    p, m, _, a = _one_step(nb, n, "bh", 0.36, kind="two_discs")
+    idx = np.random.default_rng(2).choice(n, 256, replace=False)
+    rms, mx = _rel(a[idx], oracle.direct_f64(p, m, 40.0, idx=idx))
+    print(f"config 3 vs FP64 (256 bodies): RMS {rms:.3g}, max {mx:.3g}")
+    assert np.isfinite(rms) and rms <= 3e-2, (rms, mx)
