@@ -182,6 +182,21 @@ def max_over_ranks(dist, x: float) -> float:
     return float(t.item())
 
 
+def replica_rate(dist, units: float, seconds: float) -> float:
+    """Whole-job rate of independent replicas: the units all ranks processed
+    divided by the slowest rank's time (its own time when run alone)."""
+    if dist is None:
+        return units / seconds
+    import torch
+
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    u = torch.tensor([units], dtype=torch.float64, device=dev)
+    t = torch.tensor([seconds], dtype=torch.float64, device=dev)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(u.item()) / float(t.item())
+
+
 def barrier(dist):
     if dist is not None:
         dist.barrier()
@@ -263,10 +278,10 @@ def bench_pp(args, world, rank, local, dist):
     barrier(dist)
     torch.cuda.synchronize()
     clocks = sampler.stop()
+    value = replica_rate(dist, float(n) * n * args.steps, ms / 1e3)
     ms = max_over_ranks(dist, ms)
     sec = ms / 1e3
     interactions = float(n) * n * args.steps * world
-    value = interactions / sec
 
     # dominant kernel alone: per-stage CUDA events on the launch stream
     solver.profile_enable(True)
@@ -374,9 +389,9 @@ def bench_bh(args, world, rank, local, dist):
     torch.cuda.synchronize()
     clocks = sampler.stop()
     solver.sync()
+    value = replica_rate(dist, float(n) * args.steps, ms / 1e3)
     ms = max_over_ranks(dist, ms)
     sec = ms / 1e3
-    value = float(n) * args.steps * world / sec
 
     # per-stage CUDA events on the launch stream (a separate pass)
     solver.profile_enable(True)
@@ -507,9 +522,9 @@ def bench_ensemble(args, world, rank, local, dist, steps=None):
     barrier(dist)
     clocks = sampler.stop()
     ens.sync()
+    value = replica_rate(dist, ENS_COUNT * K / ENS_STEPS, a.elapsed_time(b) / 1e3)
     ms = max_over_ranks(dist, a.elapsed_time(b))
     sec = ms / 1e3
-    value = ENS_COUNT * world * K / ENS_STEPS / sec
 
     # per-stage times of one eager step (direct sum on the side stream, concurrent)
     ens.profile_enable(True)
