@@ -225,6 +225,14 @@ int nbody_profile_read(nbody_ctx *ctx, double *ms, int *launches, int nstages);
 const char *nbody_stage_name(int stage);
 int nbody_stage_count(void);
 
+/* Self-test of the bounded device waits (no counterpart in the reference):
+ * runs a kernel on `device` whose mbarrier wait can never complete, through
+ * the bounded-wait helper the force kernels use, with a limit of limit_us
+ * microseconds (1 .. 1,000,000). The kernel gives up, so the call returns
+ * NBODY_OK with *kernel_status = NBODY_ERR_TIMEOUT and *waited_ms (may be
+ * NULL) the time it waited; the device stays usable. Synchronises the device. */
+int nbody_selftest_wait(int device, int64_t limit_us, int *kernel_status, double *waited_ms);
+
 /* ---------------------------------------------------------------- ensembles
  * Many independent systems of uneven size stepped together on one GPU (no
  * counterpart in the reference, which steps one system per process). Each

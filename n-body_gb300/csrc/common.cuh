@@ -16,6 +16,7 @@ namespace nbody {
 // L2/HBM land in microseconds, so the bound only trips on a broken invariant.
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s
 constexpr uint32_t kWaitSpinCheck = 1024;                     // polls between clock reads
+constexpr uint32_t kWaitSpinCap = 1u << 30;                   // polls at most, should the clock ever stall
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -62,17 +63,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 }
 
 // Waits for the phase with the given parity to complete, for at most
-// kWaitLimitNs. Returns false (and records NBODY_ERR_TIMEOUT) on time-out.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *status) {
+// limit_ns (and kWaitSpinCap polls). Returns false (and records
+// NBODY_ERR_TIMEOUT) on time-out.
+__device__ __forceinline__ bool mbar_wait_bounded_ns(uint64_t *bar, uint32_t parity, int *status,
+                                                     unsigned long long limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = global_ns();
-    for (uint32_t spin = 0;; ++spin) {
+    for (uint32_t spin = 0; spin < kWaitSpinCap; ++spin) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((spin % kWaitSpinCheck) == kWaitSpinCheck - 1 && global_ns() - t0 > kWaitLimitNs) {
-            record_error(status, NBODY_ERR_TIMEOUT);
-            return false;
-        }
+        if ((spin % kWaitSpinCheck) == kWaitSpinCheck - 1 && global_ns() - t0 > limit_ns) break;
     }
+    record_error(status, NBODY_ERR_TIMEOUT);
+    return false;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *status) {
+    return mbar_wait_bounded_ns(bar, parity, status, kWaitLimitNs);
 }
 
 // Orders this thread's earlier generic-proxy shared-memory accesses before

@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kSortThreads)
                 const unsigned long long t0 = global_ns();
                 uint32_t spin = 0;
                 while (((w = *dd) & ~kValueMask) == 0) {
-                    if ((++spin & 1023u) == 0 && global_ns() - t0 > kWaitLimitNs) {
+                    if (++spin >= kWaitSpinCap || ((spin & 1023u) == 0 && global_ns() - t0 > kWaitLimitNs)) {
                         record_error(status, NBODY_ERR_TIMEOUT);
                         ok = false;
                         break;

@@ -78,6 +78,7 @@ SIGNATURES = {
     "nbody_set_integrator": (_i, [_vp, _i]),
     "nbody_init_device": (_i, [_vp, _i, ctypes.c_uint64, ctypes.POINTER(_f), _i]),
     "nbody_download_masses": (_i, [_vp, _vp]),
+    "nbody_selftest_wait": (_i, [_i, _i64, _ip, ctypes.POINTER(ctypes.c_double)]),
     "nbody_ensemble_create": (_i, [ctypes.POINTER(_vp), _i, _i64]),
     "nbody_ensemble_destroy": (_i, [_vp]),
     "nbody_ensemble_last_error": (ctypes.c_char_p, [_vp]),
@@ -120,6 +121,18 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def selftest_wait(limit_us: int = 50_000, device: int = 0):
+    """Runs the bounded-wait self-test (nbody_selftest_wait): returns
+    (kernel status, milliseconds waited); the status is ERR_TIMEOUT when the
+    wait gave up as designed."""
+    st = ctypes.c_int(-1)
+    ms = ctypes.c_double(0.0)
+    rc = lib().nbody_selftest_wait(int(device), int(limit_us), ctypes.byref(st), ctypes.byref(ms))
+    if rc != OK:
+        raise NBodyError(rc, "nbody_selftest_wait")
+    return st.value, ms.value
 
 
 def status_string(status: int) -> str:
