@@ -28,7 +28,8 @@ no public dataset is involved):
        0.0035}, eps^2 U[10, 40], theta = 0.5) served by the continuous-batching
        loop under a 150 GB budget, beside FIFO one-at-a-time single-system
        solves; p50 / p99 latency and sims/s. The default line nests one rate
-       (100 req/s, 12 requests) as "serving".
+       (100 req/s, 12 requests) as "serving", and the discs workload (5 steps,
+       with its one-step CPU baseline) as "discs".
 
 A "step" is one ParticleSolver::updateParticlePositions: forces + integrator.
 value: K steps on HBM-resident state, timed with CUDA events on the launch
@@ -928,6 +929,7 @@ def main():
     ap.add_argument("--no-pp", action="store_true", help="leave the nested direct-sum measurement out")
     ap.add_argument("--no-ensemble", action="store_true", help="leave the nested ensemble measurement out")
     ap.add_argument("--no-serving", action="store_true", help="leave the nested serving measurement out")
+    ap.add_argument("--no-discs", action="store_true", help="leave the nested 16M discs measurement out")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_env()
@@ -963,6 +965,14 @@ def main():
                                                    "e2e", "clocks", "gpu_launches", "config", "plain_loop",
                                                    "speedup_vs_plain", "body_steps_per_s", "cpu_baseline")
                                 if k in en}
+        if not args.no_discs and args.workload == "bh":
+            d_args = argparse.Namespace(**vars(args))
+            d_args.workload = "discs"
+            d_args.steps = min(args.steps, 5)
+            dl = bench_bh(d_args, world, rank, local, dist)
+            line["discs"] = {k: dl[k] for k in ("component", "value", "unit", "steps", "ms_per_step", "roofline",
+                                                "e2e", "clocks", "gpu_launches", "config", "cpu_baseline")
+                             if k in dl}
         if not args.no_serving and args.workload == "bh":
             sv = bench_serving(args, world, rank, local, dist, rates=(100.0,), count=12)
             line["serving"] = {k: sv[k] for k in ("component", "value", "unit", "p50_latency_s", "p99_latency_s",
