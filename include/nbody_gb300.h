@@ -260,7 +260,7 @@ const char *nbody_ensemble_last_error(const nbody_ensemble *e);
  * stream takes that stream's priority. */
 int nbody_ensemble_set_stream(nbody_ensemble *e, void *stream);
 /* pp_shape: direct-sum launch shape 0 = 128 threads x 2 bodies, 1 = 256 x 2
- * (default), 2 = 256 x 4; key_mode: NBODY_KEYS_*. */
+ * (default), 2 = 256 x 4, 3 = 128 x 4; key_mode: NBODY_KEYS_*. */
 int nbody_ensemble_set_options(nbody_ensemble *e, int pp_shape, int key_mode);
 /* mode: NBODY_MODE_PP, NBODY_MODE_BH, or -1 (by crossover). */
 int nbody_ensemble_add(nbody_ensemble *e, int64_t n, float dt, float eps2, float theta2, int mode, int integrator,

@@ -560,7 +560,8 @@ int nbody_ensemble_set_stream(nbody_ensemble *e, void *stream) {
 }
 
 int nbody_ensemble_set_options(nbody_ensemble *e, int pp_shape, int key_mode) {
-    if (!e || pp_shape < 0 || pp_shape > 2 || (key_mode != NBODY_KEYS_OCTREE && key_mode != NBODY_KEYS_MORTON))
+    if (!e || pp_shape < 0 || pp_shape >= nbody::kPPBatchShapes ||
+        (key_mode != NBODY_KEYS_OCTREE && key_mode != NBODY_KEYS_MORTON))
         return NBODY_ERR_ARG;
     if (pp_shape != e->pp_shape) e->dirty = true;  // the work items change
     e->pp_shape = pp_shape;

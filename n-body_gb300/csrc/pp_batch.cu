@@ -22,8 +22,10 @@ namespace nbody {
 
 namespace {
 
+// K >= 4: up to 255 registers (all K accumulators and the unrolled j-pairs in
+// registers; fewer, ILP-rich warps), as the single-system kernel.
 template <int K, int T>
-__global__ void __launch_bounds__(T)
+__global__ void __launch_bounds__(T, K >= 4 ? 1 : 0)
     pp_batch_kernel(const float4 *__restrict__ pos, float4 *__restrict__ pos_out, float4 *__restrict__ vel,
                     float4 *__restrict__ acc, const int2 *__restrict__ items, int nitems,
                     const int4 *__restrict__ sys_range, const float4 *__restrict__ sys_prm,
@@ -90,11 +92,13 @@ int batch_ctas_per_sm() {
 
 }  // namespace
 
-int pp_batch_bodies_per_item(int shape) { return shape == kPPBatch128x2 ? 256 : shape == kPPBatch256x4 ? 1024 : 512; }
+int pp_batch_bodies_per_item(int shape) {
+    return shape == kPPBatch128x2 ? 256 : shape == kPPBatch256x4 ? 1024 : 512;  // 256x2 and 128x4: 512
+}
 
 int pp_batch_ctas(int shape, int device, int nitems) {
     static std::mutex mu;
-    static int cps[64][3] = {};
+    static int cps[64][kPPBatchShapes] = {};
     static int sms[64] = {};
     std::lock_guard<std::mutex> lk(mu);
     const int d = device >= 0 && device < 64 ? device : 0;
@@ -103,6 +107,7 @@ int pp_batch_ctas(int shape, int device, int nitems) {
         cps[d][kPPBatch128x2] = batch_ctas_per_sm<2, 128>();
         cps[d][kPPBatch256x2] = batch_ctas_per_sm<2, 256>();
         cps[d][kPPBatch256x4] = batch_ctas_per_sm<4, 256>();
+        cps[d][kPPBatch128x4] = batch_ctas_per_sm<4, 128>();
         if (sms[d] <= 0) sms[d] = 1;
     }
     const int resident = sms[d] * cps[d][shape];
@@ -116,6 +121,10 @@ cudaError_t pp_batch_launch(int shape, int ctas, const float4 *pos, float4 *pos_
     switch (shape) {
         case kPPBatch128x2:
             pp_batch_kernel<2, 128><<<ctas, 128, 0, st>>>(pos, pos_out, vel, acc, items, nitems, sys_range, sys_prm,
+                                                          sched, status);
+            break;
+        case kPPBatch128x4:
+            pp_batch_kernel<4, 128><<<ctas, 128, 0, st>>>(pos, pos_out, vel, acc, items, nitems, sys_range, sys_prm,
                                                           sched, status);
             break;
         case kPPBatch256x4:

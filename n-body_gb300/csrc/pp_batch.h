@@ -10,6 +10,8 @@ namespace nbody {
 constexpr int kPPBatch128x2 = 0;
 constexpr int kPPBatch256x2 = 1;
 constexpr int kPPBatch256x4 = 2;
+constexpr int kPPBatch128x4 = 3;
+constexpr int kPPBatchShapes = 4;
 
 // i-bodies per work item for a shape.
 int pp_batch_bodies_per_item(int shape);

@@ -6,8 +6,8 @@ For each size N of a grid it times ensembles of identical Plummer systems
 (enough copies to fill the GPU) once all as direct sum and once all as
 Barnes-Hut, in CUDA graphs, and takes the time per body-step; the crossover is
 where Barnes-Hut becomes cheaper (interpolated in log N between grid points).
-The launch shape is the fastest of the three on a ragged direct-sum mix below
-the crossover. Both choices keep accuracy: the direct sum is exact up to FP32
+The launch shape is the fastest on a ragged direct-sum mix (N 256 .. 16,384),
+picked first and used for the direct-sum timings. Both choices keep accuracy: the direct sum is exact up to FP32
 rounding and every Barnes-Hut system keeps its theta.
 """
 from __future__ import annotations
@@ -57,11 +57,18 @@ def time_ensemble(sizes, mode, device=0, pp_shape="256x2", steps=3, graph_steps=
 
 
 def tune(device: int = 0, grid=GRID, bodies: int = 2_000_000, verbose: bool = False) -> dict:
+    # launch shape first: a ragged direct-sum mix over the sizes the crossover can fall in
+    rng = np.random.default_rng(1)
+    mix = np.exp(rng.uniform(math.log(256), math.log(16384), 400)).astype(int)
+    shapes = {s: time_ensemble(mix, "pp", device=device, pp_shape=s) for s in PP_SHAPES}
+    best = min(shapes, key=shapes.get)
+    if verbose:
+        print("direct-sum shapes (ms per step):", {k: round(v * 1e3, 3) for k, v in shapes.items()}, flush=True)
     ns_pp, ns_bh = {}, {}
     for n in grid:
         copies = int(min(2048, max(8, bodies // n)))
         for mode, table in (("pp", ns_pp), ("bh", ns_bh)):
-            t = time_ensemble([n] * copies, mode, device=device)
+            t = time_ensemble([n] * copies, mode, device=device, pp_shape=best)
             table[n] = 1e9 * t / (copies * n)
         if verbose:
             print(f"N={n}: pp {ns_pp[n]:.3f} ns, bh {ns_bh[n]:.3f} ns per body-step", flush=True)
@@ -78,11 +85,6 @@ def tune(device: int = 0, grid=GRID, bodies: int = 2_000_000, verbose: bool = Fa
             break
     if crossover is None:
         crossover = grid[0] if ns_bh[grid[0]] < ns_pp[grid[0]] else grid[-1] * 2
-    # launch shape: a ragged direct-sum mix below the crossover
-    rng = np.random.default_rng(1)
-    mix = np.exp(rng.uniform(math.log(256), math.log(max(257, crossover)), 400)).astype(int)
-    shapes = {s: time_ensemble(mix, "pp", device=device, pp_shape=s) for s in PP_SHAPES}
-    best = min(shapes, key=shapes.get)
     return {"version": VERSION, "device_name": _device_name(device), "crossover": int(crossover), "pp_shape": best,
             "ns_per_body_step": {"pp": {str(k): round(v, 4) for k, v in ns_pp.items()},
                                  "bh": {str(k): round(v, 4) for k, v in ns_bh.items()}},

@@ -18,7 +18,7 @@ import numpy as np
 from . import (_INIT_KINDS, _MODES, INTEGRATOR_CPU, INTEGRATOR_GPU_EULER, KEYS_MORTON, KEYS_OCTREE, MODE_BH,
                MODE_PP, OK, NBodyError, ParticleSystem, _f, _i64, _ptr, lib)
 
-PP_SHAPES = {"128x2": 0, "256x2": 1, "256x4": 2}
+PP_SHAPES = {"128x2": 0, "256x2": 1, "256x4": 2, "128x4": 3}
 
 
 class Ensemble:
