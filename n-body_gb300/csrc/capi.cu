@@ -543,7 +543,7 @@ int nbody_pp_config(nbody_ctx *ctx, int64_t n, int *bodies_per_thread, int *slic
     const nbody::PPPlan plan = nbody::pp_plan(n, ctx->device);
     if (bodies_per_thread) *bodies_per_thread = plan.k;
     if (slices) *slices = plan.slices;
-    if (ctas) *ctas = plan.iblocks * plan.slices;
+    if (ctas) *ctas = plan.linear_ctas > 0 ? plan.linear_ctas : plan.iblocks * plan.slices;
     return NBODY_OK;
 }
 

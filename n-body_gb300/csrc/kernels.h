@@ -42,21 +42,22 @@ struct StageTimer {
 struct PPPlan {
     int k = 4;          // i-bodies per thread
     int threads = 128;  // threads per CTA
-    int slices = 1;     // j-slices (CTAs per i-block)
+    int slices = 1;     // j-slices (CTAs per i-block); 0 with the linear split
     int iblocks = 0;    // i-blocks of threads*k bodies
+    int linear_ctas = 0;  // > 0: linear split of the (i-block, j-pair) work over this many CTAs
     size_t arrivals_bytes = 0; // per-i-block arrival counters at the start of scratch (zeroed once)
     size_t partial_bytes = 0;  // total scratch: counters + per-slice partial accelerations
 };
 
-PPPlan pp_plan(int64_t n, int device);
+PPPlan pp_plan(int64_t n, int device, bool allow_linear = true);
 
 // pp_plan with the slice count lowered until the scratch it needs fits in
 // `scratch_bytes` (one slice needs none).
 PPPlan pp_plan_within(int64_t n, int device, size_t scratch_bytes);
 
 // Direct-sum forces at `pos` (float4 x,y,z,m) followed by the integrator
-// (or a plain force write when g.pos_out is null). When plan.slices > 1,
-// `scratch` must hold plan.partial_bytes and its first plan.arrivals_bytes
+// (or a plain force write when g.pos_out is null). When plan.slices > 1 or
+// plan.linear_ctas > 0, `scratch` must hold plan.partial_bytes and its first plan.arrivals_bytes
 // must be zero before the first launch (the kernel leaves them zero again).
 // `status` is a device int.
 cudaError_t pp_launch(const PPPlan &plan, const float4 *pos, int64_t n, float eps2, const Integrate &g,

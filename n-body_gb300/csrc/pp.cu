@@ -218,6 +218,126 @@ __global__ void __launch_bounds__(T, pp_min_blocks<K>())
     }
 }
 
+// Linear split, for the shapes that run one ILP-bound CTA per SM: the work
+// space of (i-block, j-pair) units, i-block major, is cut into gridDim.x equal
+// contiguous ranges, so every CTA evaluates the same number of pairs and no SM
+// idles for want of a CTA. With gridDim.x >= i-blocks a range covers the end of
+// one i-block and the start of the next at most: a CTA computes its (one or
+// two) segments first, publishing one partial per segment (slot 0 or 1), and
+// only then takes part in the reductions: the last CTA to arrive for an
+// i-block sums the partials of all CTAs that touched it, in CTA order
+// (deterministic), and integrates.
+__device__ __forceinline__ int64_t linear_begin(int64_t W, int64_t C, int64_t c) { return W * c / C; }
+// The CTA whose range holds unit x.
+__device__ __forceinline__ int64_t linear_cta(int64_t W, int64_t C, int64_t x) { return ((x + 1) * C + W - 1) / W - 1; }
+
+template <int K, int T, bool GUARD>
+__global__ void __launch_bounds__(T, pp_min_blocks<K>())
+    pp_force_linear_kernel(const float4 *__restrict__ pos, int64_t n, float eps2, float4 *__restrict__ partial,
+                           unsigned *__restrict__ arrivals, Integrate g, int *status) {
+    __shared__ __align__(128) float4 tile[kPPStages][kPPTile];
+    __shared__ __align__(128) float4 pairs[kPPTile];
+    __shared__ __align__(8) uint64_t full[kPPStages];
+    __shared__ int last_cta;
+    __shared__ long long s_first, s_last;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        for (int s = 0; s < kPPStages; ++s) mbar_init(&full[s], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    const Ring ring{tile, pairs, full};
+    constexpr int64_t TK = static_cast<int64_t>(T) * K;
+    const int64_t npairs = (n + 1) / 2;
+    const int64_t iblocks = (n + TK - 1) / TK;
+    const int64_t W = iblocks * npairs;
+    const int64_t C = gridDim.x, c = blockIdx.x;
+    const int64_t u0 = linear_begin(W, C, c), u1 = linear_begin(W, C, c + 1);
+    uint32_t gt = 0;
+    int64_t blocks_of[2] = {-1, -1};
+    int nseg = 0;
+    for (int64_t u = u0; u < u1; ++nseg) {
+        const int64_t b = u / npairs;
+        const int64_t p0 = u - b * npairs;
+        const int64_t pend = (npairs - p0) < (u1 - u) ? npairs : p0 + (u1 - u);
+        const int64_t j0 = 2 * p0, j1 = (2 * pend < n) ? 2 * pend : n;
+        const int64_t ib0 = b * TK;
+        if (nseg > 1) {  // cannot happen with gridDim.x >= i-blocks: report, stop
+            record_error(status, NBODY_ERR_CAPACITY);
+            return;
+        }
+        float2 nx[K], ny[K], nz[K], ax[K], ay[K], az[K];
+#pragma unroll
+        for (int r = 0; r < K; ++r) {
+            const int64_t i = ib0 + tid + r * T;
+            const float4 p = i < n ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            nx[r] = f2(-p.x, -p.x);
+            ny[r] = f2(-p.y, -p.y);
+            nz[r] = f2(-p.z, -p.z);
+            ax[r] = ay[r] = az[r] = f2(0.f, 0.f);
+        }
+        if (!item_forces<K, T, GUARD>(pos, j0, j1, nx, ny, nz, ax, ay, az, eps2, ring, gt, status)) return;
+        float4 *mine = partial + (c * 2 + nseg) * TK;
+#pragma unroll
+        for (int r = 0; r < K; ++r)
+            mine[tid + r * T] = make_float4(ax[r].x + ax[r].y, ay[r].x + ay[r].y, az[r].x + az[r].y, 0.f);
+        blocks_of[nseg] = b;
+        u = (b + 1) * npairs;
+    }
+    __threadfence();
+    __syncthreads();
+    for (int sg = 0; sg < nseg; ++sg) {
+        const int64_t b = blocks_of[sg];
+        if (tid == 0) {
+            const int64_t first = linear_cta(W, C, b * npairs), last = linear_cta(W, C, (b + 1) * npairs - 1);
+            const unsigned prev = atomicAdd(&arrivals[b], 1u);
+            last_cta = prev == static_cast<unsigned>(last - first);
+            if (last_cta) arrivals[b] = 0u;  // ready for the next launch
+            s_first = first;
+            s_last = last;
+        }
+        __syncthreads();
+        if (last_cta) {
+            __threadfence();
+            const int64_t ib0 = b * TK;
+            float fx[K], fy[K], fz[K];
+#pragma unroll
+            for (int r = 0; r < K; ++r) fx[r] = fy[r] = fz[r] = 0.f;
+            constexpr int kB = 4;  // CTAs' partials in flight at a time
+            for (int64_t c0 = s_first; c0 <= s_last; c0 += kB) {
+                float4 q[kB][K];
+#pragma unroll
+                for (int bb = 0; bb < kB; ++bb) {
+                    const int64_t cc = c0 + bb;
+                    if (cc > s_last) continue;
+                    const int64_t sl = b - linear_begin(W, C, cc) / npairs;  // the i-block's slot in CTA cc
+                    const float4 *src = partial + (cc * 2 + sl) * TK + tid;
+#pragma unroll
+                    for (int r = 0; r < K; ++r) q[bb][r] = __ldcg(src + r * T);
+                }
+#pragma unroll
+                for (int bb = 0; bb < kB; ++bb) {
+                    if (c0 + bb > s_last) continue;
+#pragma unroll
+                    for (int r = 0; r < K; ++r) {
+                        fx[r] += q[bb][r].x;
+                        fy[r] += q[bb][r].y;
+                        fz[r] += q[bb][r].z;
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < K; ++r) {
+                const int64_t i = ib0 + tid + r * T;
+                if (i >= n) continue;
+                if (g.pos_out) integrate_body(i, pos[i], fx[r], fy[r], fz[r], g);
+                else if (g.force) g.force[i] = make_float4(fx[r], fy[r], fz[r], 0.f);
+            }
+        }
+        __syncthreads();  // last_cta and s_first / s_last are rewritten for the next i-block
+    }
+}
+
 __global__ void pack_kernel(const float4 *__restrict__ positions4, const float4 *__restrict__ masses4,
                             float4 *__restrict__ pos_mass, int64_t n) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -287,7 +407,7 @@ int k_index(int k) { return k == 1 ? 0 : k == 2 ? 1 : k == 4 ? 2 : 3; }
 
 }  // namespace
 
-PPPlan pp_plan(int64_t n, int device) {
+PPPlan pp_plan(int64_t n, int device, bool allow_linear) {
     PPPlan p;
     const DeviceInfo d = device_info(device);
     // Default shapes from sweeps on GB300 (T x K in {128, 256} x {1, 2, 4, 8},
@@ -338,6 +458,24 @@ PPPlan pp_plan(int64_t n, int device) {
         if (v >= 1) best_s = static_cast<int>(std::min<int64_t>(v, std::max<int64_t>(1, npairs)));
     }
     p.slices = best_s;
+    // Shapes with one ILP-bound CTA per SM take the linear split (exactly
+    // filled SMs) from N = 32,768 on, where it measured 1-4% faster on GB300
+    // (below, the end-of-kernel reductions of every CTA cost more than the idle
+    // SMs of the sliced plan), unless a slice count is forced; NBODY_PP_LINEAR
+    // = 1 / 0 forces it on / off.
+    const char *lin = std::getenv("NBODY_PP_LINEAR");
+    const bool lin_on = lin && std::atoi(lin) == 1, lin_off = lin && std::atoi(lin) == 0;
+    const bool want_linear = allow_linear && k >= 4 && !std::getenv("NBODY_PP_SLICES") && !lin_off &&
+                             n >= static_cast<int64_t>(threads) * k && (lin_on || n >= 32768);
+    if (want_linear) {
+        const int64_t resident = sms * cps;
+        p.linear_ctas = static_cast<int>(resident * ((p.iblocks + resident - 1) / resident));
+        p.slices = 0;
+        p.arrivals_bytes = (static_cast<size_t>(p.iblocks) * sizeof(unsigned) + 255) & ~static_cast<size_t>(255);
+        p.partial_bytes = p.arrivals_bytes + static_cast<size_t>(p.linear_ctas) * 2 * static_cast<size_t>(per_block) *
+                                                 sizeof(float4);
+        return p;
+    }
     if (p.slices > 1) {
         p.arrivals_bytes = (static_cast<size_t>(p.iblocks) * sizeof(unsigned) + 255) & ~static_cast<size_t>(255);
         p.partial_bytes = p.arrivals_bytes + static_cast<size_t>(p.slices) * static_cast<size_t>(n) * sizeof(float4);
@@ -347,6 +485,7 @@ PPPlan pp_plan(int64_t n, int device) {
 
 PPPlan pp_plan_within(int64_t n, int device, size_t scratch_bytes) {
     PPPlan p = pp_plan(n, device);
+    if (p.linear_ctas > 0 && p.partial_bytes > scratch_bytes) p = pp_plan(n, device, false);
     while (p.slices > 1 && p.partial_bytes > scratch_bytes) {
         const int64_t fit = static_cast<int64_t>((scratch_bytes > p.arrivals_bytes ? scratch_bytes - p.arrivals_bytes : 0) /
                                                  (static_cast<size_t>(n) * sizeof(float4)));
@@ -361,6 +500,15 @@ PPPlan pp_plan_within(int64_t n, int device, size_t scratch_bytes) {
 template <int K, int T>
 static cudaError_t launch_kt(const PPPlan &plan, const float4 *pos, int64_t n, float eps2, const Integrate &g,
                              float4 *partial, unsigned *arrivals, cudaStream_t stream, int *status) {
+    if (plan.linear_ctas > 0) {
+        if (eps2 > 0.f)
+            pp_force_linear_kernel<K, T, false>
+                <<<plan.linear_ctas, T, 0, stream>>>(pos, n, eps2, partial, arrivals, g, status);
+        else
+            pp_force_linear_kernel<K, T, true>
+                <<<plan.linear_ctas, T, 0, stream>>>(pos, n, eps2, partial, arrivals, g, status);
+        return cudaGetLastError();
+    }
     const dim3 grid(plan.iblocks, plan.slices);
     if (eps2 > 0.f)
         pp_force_kernel<K, T, false><<<grid, T, 0, stream>>>(pos, n, eps2, plan.slices, partial, arrivals, g, status);
@@ -381,7 +529,7 @@ cudaError_t pp_launch(const PPPlan &plan, const float4 *pos, int64_t n, float ep
     if (n <= 0) return cudaSuccess;
     unsigned *arrivals = nullptr;
     float4 *partial = nullptr;
-    if (plan.slices > 1) {
+    if (plan.slices > 1 || plan.linear_ctas > 0) {
         if (!scratch) return cudaErrorInvalidValue;
         arrivals = static_cast<unsigned *>(scratch);
         partial = reinterpret_cast<float4 *>(static_cast<char *>(scratch) + plan.arrivals_bytes);

@@ -119,6 +119,28 @@ def test_pp_slicing_does_not_change_forces(nb, cuda, monkeypatch):
     check_forces(out["32"], out["1"], rms_tol=1e-6, max_tol=1e-4)
 
 
+@pytest.mark.parametrize("n", [1024, 4097, 8192, 20000])
+def test_pp_linear_split_matches_slices(nb, cuda, oracle, monkeypatch, n):
+    """The linear split of the (i-block, j-pair) work (forced here below its
+    size threshold) gives the forces of the sliced plan and of the port."""
+    from nbody_gb300 import initializers as I
+
+    pos, vel, mass = I.uniform_ball(n, seed=n + 7)
+    out = {}
+    for lin in ("1", "0"):
+        monkeypatch.setenv("NBODY_PP_LINEAR", lin)
+        monkeypatch.setenv("NBODY_PP_K", "4")
+        solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp")
+        cfg = solver.pp_config()
+        assert (cfg["slices"] == 0) == (lin == "1"), cfg
+        sysm = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+        solver.update_particle_positions(sysm)
+        out[lin] = sysm.forces.copy()
+        solver.close()
+    check_forces(out["1"], out["0"], rms_tol=1e-6, max_tol=1e-4)
+    check_forces(out["1"], oracle.pp_forces(pos, mass, 40.0))
+
+
 @pytest.mark.parametrize("threads", ["128", "256"])
 @pytest.mark.parametrize("k", ["1", "2", "4", "8"])
 def test_pp_bodies_per_thread_variants(nb, cuda, oracle, monkeypatch, k, threads):
