@@ -150,7 +150,7 @@ int nbody_diagnostics(nbody_ctx *ctx, double *out);
 /* Seeded initial conditions generated on the GPU straight into the resident
  * state, in place of nbody_upload (same effect: the next nbody_step starts from
  * them; body i is caller index i for nbody_download). The reference's
- * initialisers (src/ParticleSystemInitializer/*, chosen by -i in
+ * initialisers (the files under src/ParticleSystemInitializer/, chosen by -i in
  * src/main.cpp:41-66) seed from the clock or std::random_device; these restate
  * their shapes with a counter-based generator, so a (kind, seed, params, n)
  * always gives the same bits. Kinds 1, 2, 4, 5, 6 keep the reference's -i
