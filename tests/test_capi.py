@@ -58,3 +58,31 @@ def test_create_fails_loudly_without_gpu(nb):
     with pytest.raises(nb.NBodyError) as e:
         nb.ParticleSolverCUDA(0.01, 1.0, 128)
     assert e.value.status in (nb.ERR_CUDA, nb.ERR_NOMEM)
+
+
+def test_header_is_plain_c_and_links(nb, tmp_path):
+    """include/nbody_gb300.h compiles as C99 with warnings as errors, and a C
+    program that takes the address of every declared function links against
+    the library (what a cgo / FFI binding needs)."""
+    import re
+    import shutil
+    import subprocess
+
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc missing")
+    hdr = os.path.join(ROOT, "include", "nbody_gb300.h")
+    names = sorted(set(re.findall(r"^[a-z_ ]*?\*?\s*(nbody_\w+)\(", open(hdr).read(), re.M)))
+    assert len(names) > 30
+    src = tmp_path / "use.c"
+    src.write_text('#include "nbody_gb300.h"\n#include <stdio.h>\ntypedef void (*fn)(void);\n'
+                   "int main(void) {\n    fn f[] = {" + ", ".join(f"(fn){n}" for n in names) +
+                   "};\n    printf(\"%d %s\\n\", (int)(sizeof f / sizeof f[0]), nbody_status_string(NBODY_ERR_ARG));\n"
+                   "    return 0;\n}\n")
+    exe = tmp_path / "use"
+    libdir = os.path.dirname(nb.LIB_PATH)
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", f"-I{ROOT}/include", str(src),
+                        "-o", str(exe), f"-L{libdir}", "-lnbody_gb300", f"-Wl,-rpath,{libdir}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0 and out.stdout.split()[0] == str(len(names))
