@@ -56,6 +56,23 @@ def time_ensemble(sizes, mode, device=0, pp_shape="256x2", steps=3, graph_steps=
         return (time.perf_counter() - t0) / steps
 
 
+def crossover_from(grid, ns_pp: dict, ns_bh: dict) -> int:
+    """The size from which Barnes-Hut is cheaper per body-step than the direct
+    sum: the first grid point where it is, log-interpolated between that point
+    and the one before; the grid's first point if Barnes-Hut always wins, twice
+    its last if it never does."""
+    grid = list(grid)
+    if ns_bh[grid[0]] < ns_pp[grid[0]]:
+        return int(grid[0])
+    for a, b in zip(grid, grid[1:]):
+        if ns_bh[b] < ns_pp[b]:
+            # log(pp / bh) rises from <= 0 at a to > 0 at b
+            ra, rb = math.log(ns_pp[a] / ns_bh[a]), math.log(ns_pp[b] / ns_bh[b])
+            f = ra / (ra - rb)
+            return int(round(math.exp(math.log(a) + f * (math.log(b) - math.log(a)))))
+    return int(grid[-1] * 2)
+
+
 def tune(device: int = 0, grid=GRID, bodies: int = 2_000_000, verbose: bool = False) -> dict:
     # launch shape first: a ragged direct-sum mix over the sizes the crossover can fall in
     rng = np.random.default_rng(1)
@@ -72,19 +89,7 @@ def tune(device: int = 0, grid=GRID, bodies: int = 2_000_000, verbose: bool = Fa
             table[n] = 1e9 * t / (copies * n)
         if verbose:
             print(f"N={n}: pp {ns_pp[n]:.3f} ns, bh {ns_bh[n]:.3f} ns per body-step", flush=True)
-    crossover = None
-    for a, b in zip(grid, grid[1:]):
-        if ns_bh[a] < ns_pp[a]:
-            crossover = a
-            break
-        if ns_bh[b] < ns_pp[b]:
-            # log-linear interpolation of log(pp / bh) between a and b
-            ra, rb = math.log(ns_pp[a] / ns_bh[a]), math.log(ns_pp[b] / ns_bh[b])
-            f = ra / (ra - rb)
-            crossover = int(round(math.exp(math.log(a) + f * (math.log(b) - math.log(a)))))
-            break
-    if crossover is None:
-        crossover = grid[0] if ns_bh[grid[0]] < ns_pp[grid[0]] else grid[-1] * 2
+    crossover = crossover_from(grid, ns_pp, ns_bh)
     return {"version": VERSION, "device_name": _device_name(device), "crossover": int(crossover), "pp_shape": best,
             "ns_per_body_step": {"pp": {str(k): round(v, 4) for k, v in ns_pp.items()},
                                  "bh": {str(k): round(v, 4) for k, v in ns_bh.items()}},
