@@ -12,10 +12,11 @@
 // non-tensor TMA bulk copy into a 3-stage ring completed on mbarriers; each
 // landed tile is re-laid as j-pairs. The inner loop takes two j-bodies at a
 // time so that every FP32 instruction is a packed f32x2 one
-// (FADD2/FFMA2/FMUL2): 12 packed ops + 2 MUFU.RSQ per pair of interactions. j-slices exist to fill 152 SMs when n is small; their partial
-// accelerations are summed in slice order by a second kernel (deterministic)
-// which also applies the integrator. With one slice the integrator runs in the
-// force kernel's epilogue.
+// (FADD2/FFMA2/FMUL2): 12 packed ops + 2 MUFU.RSQ per pair of interactions.
+// j-slices exist to fill 152 SMs when n is small; the CTA that completes an
+// i-block last sums its slices' partial accelerations in slice order
+// (deterministic) and applies the integrator. With one slice the integrator
+// runs in the force kernel's epilogue.
 //
 // Self-interaction: the reference skips j == i by index. Here the i == j term
 // has dx = 0 and contributes exactly 0 when eps2 > 0; with eps2 == 0 the GUARD
@@ -47,10 +48,10 @@ __global__ void __launch_bounds__(T, pp_min_blocks<K>())
     pp_force_kernel(const float4 *__restrict__ pos, int64_t n, float eps2, int nslices,
                     float4 *__restrict__ partial, unsigned *__restrict__ arrivals, Integrate g, int *status) {
     // tile: TMA landing zone, bodies as float4 (x, y, z, m).
-    // pairs: the current tile re-laid as j-pairs {x0 x1 y0 y1}{z0 z1 m0 m1}, so
-    // that one 16-byte shared load yields two packed f32x2 operands.
+    // pairs: two tiles re-laid as j-pairs {x0 x1 y0 y1}{z0 z1 m0 m1}, so that
+    // one 16-byte shared load yields two packed f32x2 operands.
     __shared__ __align__(128) float4 tile[kPPStages][kPPTile];
-    __shared__ __align__(128) float4 pairs[kPPTile];
+    __shared__ __align__(128) float4 pairs[2][kPPTile];
     __shared__ __align__(8) uint64_t full[kPPStages];
     __shared__ int last_cta;
 
@@ -66,6 +67,24 @@ __global__ void __launch_bounds__(T, pp_min_blocks<K>())
     const int64_t len = j1 > j0 ? j1 - j0 : 0;
     const int ntiles = static_cast<int>((len + kPPTile - 1) / kPPTile);
 
+    // Producer: thread 0 fetches tile t of this slice into stage t % kPPStages.
+    auto issue = [&](int t) {
+        const int stage = t % kPPStages;
+        const int64_t jt = j0 + static_cast<int64_t>(t) * kPPTile;
+        const int cnt = static_cast<int>((j1 - jt) < kPPTile ? (j1 - jt) : kPPTile);
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&full[stage], static_cast<uint32_t>(cnt) * 16u);
+        tma_bulk_g2s(&tile[stage][0], pos + jt, static_cast<uint32_t>(cnt) * 16u, &full[stage]);
+    };
+    // The first tiles are requested before the i-bodies are loaded, so that
+    // the two memory latencies overlap; the barrier below publishes the
+    // mbarrier initialisation to the other threads before any of them waits.
+    if (tid == 0) {
+        for (int s = 0; s < kPPStages; ++s) mbar_init(&full[s], 1);
+        mbar_init_fence();
+        for (int t = 0; t < kPPStages && t < ntiles; ++t) issue(t);
+    }
+
     float2 nx[K], ny[K], nz[K], ax[K], ay[K], az[K];
     float4 pi[K];
 #pragma unroll
@@ -78,49 +97,45 @@ __global__ void __launch_bounds__(T, pp_min_blocks<K>())
         ax[r] = ay[r] = az[r] = f2(0.f, 0.f);
     }
     const float2 e2 = f2(eps2, eps2);
-
-    if (tid == 0) {
-        for (int s = 0; s < kPPStages; ++s) mbar_init(&full[s], 1);
-        mbar_init_fence();
-    }
     __syncthreads();
 
-    // Producer: thread 0 fetches tile t of this slice into stage t % kPPStages.
-    auto issue = [&](int t) {
-        const int stage = t % kPPStages;
-        const int64_t jt = j0 + static_cast<int64_t>(t) * kPPTile;
-        const int cnt = static_cast<int>((j1 - jt) < kPPTile ? (j1 - jt) : kPPTile);
-        fence_proxy_async_smem();
-        mbar_arrive_expect_tx(&full[stage], static_cast<uint32_t>(cnt) * 16u);
-        tma_bulk_g2s(&tile[stage][0], pos + jt, static_cast<uint32_t>(cnt) * 16u, &full[stage]);
-    };
-    if (tid == 0) {
-        for (int t = 0; t < kPPStages && t < ntiles; ++t) issue(t);
-    }
-
-    bool failed = false;
-    int t = 0;
-    for (; t < ntiles; ++t) {
+    // Waits for tile t and re-lays it as j-pairs into pairs[t & 1] (an odd
+    // last body is paired with m = 0). Returns false if the copy never landed.
+    auto stage_in = [&](int t) -> bool {
         const int stage = t % kPPStages;
         const uint32_t parity = static_cast<uint32_t>(t / kPPStages) & 1u;
-        const bool ok = mbar_wait_bounded(&full[stage], parity, status);
-        if (!__syncthreads_and(ok)) {  // also: every thread is done with `pairs`
-            failed = true;
-            break;
-        }
+        if (!mbar_wait_bounded(&full[stage], parity, status)) return false;
         const int64_t jt = j0 + static_cast<int64_t>(t) * kPPTile;
         const int cnt = static_cast<int>((j1 - jt) < kPPTile ? (j1 - jt) : kPPTile);
         const int npr = (cnt + 1) >> 1;
-        // Re-lay the tile as j-pairs; an odd last body is paired with m = 0.
+        float4 *dst = pairs[t & 1];
         for (int q = tid; q < npr; q += T) {
             const float4 a = tile[stage][2 * q];
             const float4 b = (2 * q + 1 < cnt) ? tile[stage][2 * q + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
-            pairs[2 * q] = make_float4(a.x, b.x, a.y, b.y);
-            pairs[2 * q + 1] = make_float4(a.z, b.z, a.w, b.w);
+            dst[2 * q] = make_float4(a.x, b.x, a.y, b.y);
+            dst[2 * q + 1] = make_float4(a.z, b.z, a.w, b.w);
         }
-        __syncthreads();  // pairs ready; tile[stage] is free again
-        if (tid == 0 && t + kPPStages < ntiles) issue(t + kPPStages);
-        const float4 *pr = pairs;
+        return true;
+    };
+
+    // Tile t is computed from pairs[t & 1] while tile t + 1 is re-laid into
+    // the other buffer: one block barrier per tile. After the barrier that
+    // ends tile t, tile t + 1's ring stage is free and takes tile t + 1 + stages.
+    bool failed = false;
+    int fail_at = 0;  // first tile whose copy may still be in flight
+    if (ntiles > 0) {
+        if (!__syncthreads_and(stage_in(0))) {
+            failed = true;
+        } else if (tid == 0 && kPPStages < ntiles) {
+            issue(kPPStages);
+        }
+    }
+    for (int t = 0; t < ntiles && !failed; ++t) {
+        const bool ok = (t + 1 < ntiles) ? stage_in(t + 1) : true;
+        const int64_t jt = j0 + static_cast<int64_t>(t) * kPPTile;
+        const int cnt = static_cast<int>((j1 - jt) < kPPTile ? (j1 - jt) : kPPTile);
+        const int npr = (cnt + 1) >> 1;
+        const float4 *pr = pairs[t & 1];
 #pragma unroll 2
         for (int q = 0; q < npr; ++q) {
             const float4 u = pr[2 * q];
@@ -146,12 +161,18 @@ __global__ void __launch_bounds__(T, pp_min_blocks<K>())
                 az[r] = __ffma2_rn(dz, s, az[r]);
             }
         }
+        if (!__syncthreads_and(ok)) {  // also: every thread is done with pairs[t & 1]
+            failed = true;
+            fail_at = t + 1;
+            break;
+        }
+        if (tid == 0 && t + 1 + kPPStages < ntiles) issue(t + 1 + kPPStages);
     }
 
     if (failed) {
         // Drain this CTA's copies still in flight before shared memory goes away.
         if (tid == 0) {
-            for (int u = t; u < ntiles && u < t + kPPStages; ++u)
+            for (int u = fail_at; u < ntiles && u < fail_at + kPPStages; ++u)
                 mbar_wait_bounded(&full[u % kPPStages], static_cast<uint32_t>(u / kPPStages) & 1u, status);
         }
         __syncthreads();
@@ -192,29 +213,41 @@ __global__ void __launch_bounds__(T, pp_min_blocks<K>())
     __syncthreads();
     if (!last_cta) return;
     __threadfence();
-    constexpr int kBatch = 8;  // partial loads in flight per body
+    // kBatch slices x K bodies of partial loads in flight at once (16 float4),
+    // each body still summed in slice order.
+    constexpr int kBatch = K >= 16 ? 1 : 16 / K;
+    float fx[K], fy[K], fz[K];
+#pragma unroll
+    for (int r = 0; r < K; ++r) fx[r] = fy[r] = fz[r] = 0.f;
+    for (int sl0 = 0; sl0 < nslices; sl0 += kBatch) {
+        float4 q[kBatch][K];
+#pragma unroll
+        for (int b = 0; b < kBatch; ++b) {
+#pragma unroll
+            for (int r = 0; r < K; ++r) {
+                const int64_t i = ib0 + tid + r * T;
+                q[b][r] = (sl0 + b < nslices && i < n) ? __ldcg(&partial[static_cast<int64_t>(sl0 + b) * n + i])
+                                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < kBatch; ++b) {
+            if (sl0 + b < nslices) {
+#pragma unroll
+                for (int r = 0; r < K; ++r) {
+                    fx[r] += q[b][r].x;
+                    fy[r] += q[b][r].y;
+                    fz[r] += q[b][r].z;
+                }
+            }
+        }
+    }
 #pragma unroll
     for (int r = 0; r < K; ++r) {
         const int64_t i = ib0 + tid + r * T;
         if (i >= n) continue;
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        for (int sl0 = 0; sl0 < nslices; sl0 += kBatch) {
-            float4 q[kBatch];
-#pragma unroll
-            for (int b = 0; b < kBatch; ++b)
-                q[b] = (sl0 + b < nslices) ? __ldcg(&partial[static_cast<int64_t>(sl0 + b) * n + i])
-                                           : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-            for (int b = 0; b < kBatch; ++b) {
-                if (sl0 + b < nslices) {
-                    fx += q[b].x;
-                    fy += q[b].y;
-                    fz += q[b].z;
-                }
-            }
-        }
-        if (g.pos_out) integrate_body(i, pi[r], fx, fy, fz, g);
-        else if (g.force) g.force[i] = make_float4(fx, fy, fz, 0.f);
+        if (g.pos_out) integrate_body(i, pi[r], fx[r], fy[r], fz[r], g);
+        else if (g.force) g.force[i] = make_float4(fx[r], fy[r], fz[r], 0.f);
     }
 }
 
@@ -437,8 +470,11 @@ PPPlan pp_plan(int64_t n, int device, bool allow_linear) {
     // Slice count: each slice keeps at least one full tile of j-bodies. The
     // cost model charges every SM for the waves of CTAs it must run (a partial
     // wave costs a full one, since a lone CTA cannot fill an SM), each CTA for
-    // its j-pairs plus a fixed overhead (pipeline fill, i-loads, epilogue), and
-    // the final sum for reading one partial per slice.
+    // its j-pairs plus a fixed overhead (pipeline fill, i-loads, epilogue: about
+    // 24 pairs' time), and the final sum for reading one partial per slice
+    // (about one pair's time: the loads of 16 / K slices are in flight at once).
+    // On GB300 at N = 16,384 this takes 19 slices in two full waves over 152 SMs
+    // (110.7 us) over 9 slices in one wave over 144 SMs (112.0 us).
     int64_t smax = std::max<int64_t>(1, std::min<int64_t>(npairs / (kPPTile / 2), 64));
     double best = 1e300;
     int best_s = 1;
@@ -446,8 +482,8 @@ PPPlan pp_plan(int64_t n, int device, bool allow_linear) {
         const int64_t total = static_cast<int64_t>(p.iblocks) * sl;
         const int64_t per_sm = (total + sms - 1) / sms;
         const int64_t waves = (per_sm + cps - 1) / cps;
-        const double cta_cost = static_cast<double>(npairs) / static_cast<double>(sl) + 128.0;
-        const double cost = static_cast<double>(waves * cps) * cta_cost + 8.0 * static_cast<double>(sl);
+        const double cta_cost = static_cast<double>(npairs) / static_cast<double>(sl) + 24.0;
+        const double cost = static_cast<double>(waves * cps) * cta_cost + static_cast<double>(sl);
         if (cost < best * (1.0 - 1e-9)) {
             best = cost;
             best_s = static_cast<int>(sl);
