@@ -97,7 +97,10 @@ float nbody_get_squared_softening(const nbody_ctx *ctx);
  * positions, velocities, accelerations (and forces4, which may be NULL) back
  * before returning. forces4 receives the acceleration evaluated at the
  * positions the last step started from, as the reference's forces[] array.
- * Pinned host memory makes the copies asynchronous DMA; pageable memory works. */
+ * Page-locked host memory (cudaHostAlloc / cudaMallocHost, or registered and
+ * mapped) is read and written in place by one kernel each way over the
+ * host-device link; pageable memory goes through one copy per array. Both
+ * move the same values. */
 int nbody_update_host(nbody_ctx *ctx, float *positions4, float *velocities4, float *accelerations4,
                       const float *masses4, float *forces4, int steps);
 

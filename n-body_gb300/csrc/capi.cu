@@ -92,6 +92,21 @@ int fail(nbody_ctx *ctx, cudaError_t e) {
 
 bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
+// The device-mapped address of a page-locked host buffer (cudaHostAlloc /
+// cudaMallocHost, or cudaHostRegister'ed and mapped), or nullptr for any other
+// pointer: pageable memory, device memory, or an address not 16-byte aligned.
+// Only such addresses are handed to the host_gather / host_scatter kernels.
+float4 *mapped(const void *p) {
+    if (!p || !aligned16(p)) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer || !aligned16(a.devicePointer)) return nullptr;
+    return static_cast<float4 *>(a.devicePointer);
+}
+
 int ensure_scratch(nbody_ctx *ctx, size_t bytes) {
     if (bytes <= ctx->scratch_bytes) return NBODY_OK;
     if (ctx->scratch) {
@@ -318,21 +333,30 @@ int nbody_upload(nbody_ctx *ctx, const float *positions4, const float *velocitie
     if (!ctx || !positions4 || !masses4) return NBODY_ERR_ARG;
     DeviceGuard dg(ctx->device);
     const size_t b4 = static_cast<size_t>(ctx->n) * sizeof(float4);
-    NB_CK(ctx, cudaMemcpyAsync(ctx->stage, positions4, b4, cudaMemcpyHostToDevice, ctx->stream));
-    NB_CK(ctx, cudaMemcpyAsync(ctx->stage + ctx->n, masses4, b4, cudaMemcpyHostToDevice, ctx->stream));
-    if (velocities4)
-        NB_CK(ctx, cudaMemcpyAsync(ctx->vel, velocities4, b4, cudaMemcpyHostToDevice, ctx->stream));
-    else
-        NB_CK(ctx, cudaMemsetAsync(ctx->vel, 0, b4, ctx->stream));
-    if (accelerations4)
-        NB_CK(ctx, cudaMemcpyAsync(ctx->acc, accelerations4, b4, cudaMemcpyHostToDevice, ctx->stream));
-    else
-        NB_CK(ctx, cudaMemsetAsync(ctx->acc, 0, b4, ctx->stream));
+    // Page-locked host buffers are read in place by one kernel; otherwise one
+    // copy per array into the staging area, then the pack kernel.
+    const float4 *mp = mapped(positions4), *mm = mapped(masses4);
+    const float4 *mv = velocities4 ? mapped(velocities4) : nullptr;
+    const float4 *ma = accelerations4 ? mapped(accelerations4) : nullptr;
+    if (mp && mm && (!velocities4 || mv) && (!accelerations4 || ma)) {
+        NB_CK(ctx, nbody::host_gather(mp, mm, mv, ma, ctx->pos[0], ctx->vel, ctx->acc, ctx->n, ctx->stream));
+    } else {
+        NB_CK(ctx, cudaMemcpyAsync(ctx->stage, positions4, b4, cudaMemcpyHostToDevice, ctx->stream));
+        NB_CK(ctx, cudaMemcpyAsync(ctx->stage + ctx->n, masses4, b4, cudaMemcpyHostToDevice, ctx->stream));
+        if (velocities4)
+            NB_CK(ctx, cudaMemcpyAsync(ctx->vel, velocities4, b4, cudaMemcpyHostToDevice, ctx->stream));
+        else
+            NB_CK(ctx, cudaMemsetAsync(ctx->vel, 0, b4, ctx->stream));
+        if (accelerations4)
+            NB_CK(ctx, cudaMemcpyAsync(ctx->acc, accelerations4, b4, cudaMemcpyHostToDevice, ctx->stream));
+        else
+            NB_CK(ctx, cudaMemsetAsync(ctx->acc, 0, b4, ctx->stream));
+        NB_CK(ctx, nbody::pack_state(ctx->stage, ctx->stage + ctx->n, ctx->pos[0], ctx->n, ctx->stream));
+    }
     ctx->cur = 0;
     ctx->bh_pos = 0;
     ctx->bh_va = 0;
     ctx->ids_valid = false;
-    NB_CK(ctx, nbody::pack_state(ctx->stage, ctx->stage + ctx->n, ctx->pos[0], ctx->n, ctx->stream));
     ctx->uploaded = true;
     return NBODY_OK;
 }
@@ -351,6 +375,24 @@ int nbody_download(nbody_ctx *ctx, float *positions4, float *velocities4, float 
     DeviceGuard dg(ctx->device);
     const size_t b4 = static_cast<size_t>(ctx->n) * sizeof(float4);
     const int64_t n = ctx->n;
+    {
+        // Page-locked host buffers are written in place by one kernel, in the
+        // caller's order (through the inverse of the sorted order, built in the
+        // staging area, when the state is sorted).
+        float4 *mp = positions4 ? mapped(positions4) : nullptr, *mv = velocities4 ? mapped(velocities4) : nullptr;
+        float4 *ma = accelerations4 ? mapped(accelerations4) : nullptr, *mf = forces4 ? mapped(forces4) : nullptr;
+        if ((!positions4 || mp) && (!velocities4 || mv) && (!accelerations4 || ma) && (!forces4 || mf)) {
+            const bool bh = ctx->mode == NBODY_MODE_BH;
+            const int *ids = (bh && ctx->ids_valid) ? ctx->ids[ctx->bh_va] : nullptr;
+            if (mp || mv || ma || mf)
+                NB_CK(ctx, nbody::host_scatter(bh ? ctx->pos[ctx->bh_pos] : ctx->pos[ctx->cur],
+                                               bh ? ctx->vel2[ctx->bh_va] : ctx->vel,
+                                               bh ? ctx->acc2[ctx->bh_va] : ctx->acc, ids,
+                                               reinterpret_cast<int *>(ctx->stage), mp, mv, ma, mf, n, ctx->stream,
+                                               ctx->status));
+            return read_status(ctx);
+        }
+    }
     if (ctx->mode == NBODY_MODE_BH && ctx->ids_valid) {
         // Resident state is in the last sort's order: scatter back by id.
         const int *ids = ctx->ids[ctx->bh_va];

@@ -70,5 +70,15 @@ cudaError_t unpack_positions(const float4 *pos_mass, float4 *positions4, int64_t
 // masses4[ids ? ids[i] : i] = (m_i, 0, 0, 0): the reference's vec4 mass layout.
 cudaError_t unpack_masses(const float4 *pos_mass, const int *ids, float4 *masses4, int64_t n, cudaStream_t stream,
                           int *status);
+// The same moves straight between device state and page-locked host buffers,
+// given their device-mapped addresses (hostio.cu): vel_h / acc_h may be null
+// (zeros in); any output may be null; with ids (device) the state is in sorted
+// order and out[ids[i]] = in[i], through the inverse order built in `inv`
+// (n ints of device scratch).
+cudaError_t host_gather(const float4 *positions4, const float4 *masses4, const float4 *vel_h, const float4 *acc_h,
+                        float4 *pos_mass, float4 *vel, float4 *acc, int64_t n, cudaStream_t stream);
+cudaError_t host_scatter(const float4 *pos_mass, const float4 *vel, const float4 *acc, const int *ids, int *inv,
+                         float4 *positions4, float4 *vel_h, float4 *acc_h, float4 *force_h, int64_t n,
+                         cudaStream_t stream, int *status);
 
 }  // namespace nbody

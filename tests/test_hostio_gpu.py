@@ -1,0 +1,97 @@
+"""Host-layout calls with page-locked host buffers.
+
+nbody_upload / nbody_download read and write page-locked, mapped host buffers
+in place with one kernel each (n-body_gb300/csrc/hostio.cu) instead of a
+cudaMemcpyAsync per array; pageable buffers keep the copy path. Both paths
+move the same values: every array must match bit for bit, for the direct sum
+and for Barnes-Hut (whose resident state is in sorted order and is scattered
+back through the body ids), and when only some buffers are page-locked.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _pin(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
+
+def _system(nb, torch, pos, vel, mass, pinned):
+    s = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+    if pinned == "all":
+        for name in ("positions", "velocities", "accelerations", "masses", "forces"):
+            setattr(s, name, _pin(torch, getattr(s, name)))
+    elif pinned == "some":
+        s.positions = _pin(torch, s.positions)
+        s.forces = _pin(torch, s.forces)
+    return s
+
+
+def _same(a, b):
+    for name in ("positions", "velocities", "accelerations", "forces"):
+        np.testing.assert_array_equal(getattr(a, name), getattr(b, name), err_msg=name)
+
+
+@pytest.mark.parametrize("mode,n,steps", [("pp", 5000, 3), ("pp", 1, 1), ("bh", 20000, 2), ("bh", 777, 3)])
+def test_pinned_and_pageable_paths_agree(nb, cuda, mode, n, steps):
+    torch = cuda
+    from nbody_gb300 import initializers as I
+
+    pos, vel, mass = I.plummer(n, a=50.0, seed=n) if n > 1 else I.uniform_ball(n, seed=1)
+    out = {}
+    for pinned in ("none", "all", "some"):
+        s = _system(nb, torch, pos, vel, mass, pinned)
+        solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode=mode, theta2=0.25)
+        solver.update_particle_positions(s, steps=steps)
+        solver.update_particle_positions(s)  # host state in, again
+        solver.close()
+        out[pinned] = s
+    _same(out["all"], out["none"])
+    _same(out["some"], out["none"])
+    assert np.all(out["all"].positions[:, 3] == 0)
+
+
+def test_resident_download_to_pinned_after_sorted_steps(nb, cuda):
+    """Barnes-Hut state stays in sorted order between steps; a download into
+    page-locked buffers must scatter it back to the caller's order."""
+    torch = cuda
+    from nbody_gb300 import initializers as I
+
+    n = 12345
+    pos, vel, mass = I.plummer(n, a=100.0, seed=9)
+    solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="bh", theta2=0.25)
+    solver.upload(_system(nb, torch, pos, vel, mass, "all"))
+    solver.step(4)
+    a = _system(nb, torch, np.zeros_like(pos), np.zeros_like(vel), mass, "none")
+    b = _system(nb, torch, np.zeros_like(pos), np.zeros_like(vel), mass, "all")
+    solver.download(a)
+    solver.download(b)
+    solver.close()
+    _same(a, b)
+
+
+def test_upload_without_velocities_zeroes_them(nb, cuda):
+    """nbody_upload with null velocity / acceleration buffers starts them at
+    zero on both paths."""
+    torch = cuda
+    from nbody_gb300 import initializers as I
+
+    n = 3000
+    pos, vel, mass = I.uniform_ball(n, seed=4)
+    res = []
+    for pinned in ("none", "all"):
+        s = _system(nb, torch, pos, vel + 1.0, mass, pinned)
+        solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp")
+        p = lambda a: ctypes.c_void_p(a.ctypes.data)  # noqa: E731
+        assert nb.lib().nbody_upload(solver._ctx, p(s.positions), None, None, p(s.masses)) == nb.OK
+        solver.step(1)
+        solver.download(s)
+        solver.close()
+        res.append(s)
+    _same(res[0], res[1])
+    ref = nb.ParticleSystem(pos.copy(), np.zeros_like(vel), mass)
+    nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp").update_particle_positions(ref)
+    np.testing.assert_array_equal(res[0].positions, ref.positions)
