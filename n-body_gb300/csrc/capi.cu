@@ -36,6 +36,7 @@ struct nbody_ctx {
     float4 *acc = nullptr;
     float4 *stage = nullptr;  // 2n float4: reference-layout positions, then masses
     int *status = nullptr;    // device status word
+    int *status_host = nullptr;  // page-locked copy of it, read after a stream sync
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     bool uploaded = false;
@@ -123,9 +124,16 @@ int ensure_scratch(nbody_ctx *ctx, size_t bytes) {
 
 int read_status(nbody_ctx *ctx) {
     int h = NBODY_OK;
-    NB_CK(ctx, cudaMemcpyAsync(&h, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    NB_CK(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream));
-    NB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->status_host) {
+        NB_CK(ctx, cudaMemcpyAsync(ctx->status_host, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        NB_CK(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream));
+        NB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        h = *ctx->status_host;
+    } else {
+        NB_CK(ctx, cudaMemcpyAsync(&h, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        NB_CK(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream));
+        NB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    }
     if (h != NBODY_OK && ctx->scratch) {
         // A kernel gave up part-way: its arrival counters may be left non-zero.
         NB_CK(ctx, cudaMemsetAsync(ctx->scratch, 0, ctx->scratch_bytes, ctx->stream));
@@ -265,6 +273,10 @@ int nbody_create(nbody_ctx **out, int device, int mode, int64_t n, float dt, flo
     alloc(reinterpret_cast<void **>(&ctx->acc), b4);
     alloc(reinterpret_cast<void **>(&ctx->stage), 2 * b4);
     alloc(reinterpret_cast<void **>(&ctx->status), sizeof(int));
+    if (rc == NBODY_OK && cudaMallocHost(reinterpret_cast<void **>(&ctx->status_host), sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();  // the status is then read into pageable memory
+        ctx->status_host = nullptr;
+    }
     if (mode == NBODY_MODE_BH) {
         ctx->vel2[0] = ctx->vel;
         ctx->acc2[0] = ctx->acc;
@@ -303,6 +315,7 @@ int nbody_destroy(nbody_ctx *ctx) {
         cudaFree(ctx->acc);
         cudaFree(ctx->stage);
         cudaFree(ctx->status);
+        if (ctx->status_host) cudaFreeHost(ctx->status_host);
         cudaFree(ctx->scratch);
         cudaFree(ctx->vel2[1]);
         cudaFree(ctx->acc2[1]);
