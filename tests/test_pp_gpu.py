@@ -141,6 +141,20 @@ def test_pp_linear_split_matches_slices(nb, cuda, oracle, monkeypatch, n):
     check_forces(out["1"], oracle.pp_forces(pos, mass, 40.0))
 
 
+def test_pp_plan_runs_full_waves_at_16384(nb, cuda):
+    """On a 152-SM GB300 the slice model fills every SM in every wave at the
+    16,384-body workload: 19 slices x 16 i-blocks = 304 CTAs, two full waves of
+    one CTA per SM."""
+    torch = cuda
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    if sms != 152:
+        pytest.skip(f"plan pinned for 152 SMs, device has {sms}")
+    cfg = nb.ParticleSolverCUDA(0.0035, 40.0, 16384, mode="pp").pp_config()
+    assert cfg["bodies_per_thread"] == 4
+    assert cfg["ctas"] % sms == 0 and cfg["ctas"] // sms == 2, cfg
+    assert cfg["slices"] == 19, cfg
+
+
 @pytest.mark.parametrize("threads", ["128", "256"])
 @pytest.mark.parametrize("k", ["1", "2", "4", "8"])
 def test_pp_bodies_per_thread_variants(nb, cuda, oracle, monkeypatch, k, threads):
