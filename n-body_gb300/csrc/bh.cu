@@ -33,7 +33,10 @@
 // evaluated without FMA contraction (Octree.cpp:303-338).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cfloat>
+#include <cstdlib>
+#include <cstring>
 
 #include "bh.h"
 #include "common.cuh"
@@ -468,7 +471,8 @@ __device__ __forceinline__ int octree_parent(const BinaryTree &t, const uint32_t
 
 __global__ void emit_cells_kernel(const uint64_t *__restrict__ k, int64_t n, BinaryTree t,
                                   const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
-                                  const float *__restrict__ box, BHNode *__restrict__ nodes, Records r, SegView sv) {
+                                  const float *__restrict__ box, BHNode *__restrict__ nodes, Records r, SegView sv,
+                                  bool parents) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     if (!t.top[i]) return;
@@ -485,14 +489,16 @@ __global__ void emit_cells_kernel(const uint64_t *__restrict__ k, int64_t n, Bin
     }
     nodes[idx].meta = meta;
     r.level[idx] = L;
-    const int par = i == 0 ? -1 : octree_parent(t, mask, P, t.iparent[i], base);
-    r.parent[idx] = par;
-    if (par >= 0) atomicAdd(&r.nchild[par], 1);
+    if (parents) {  // the climbing upsweep's links
+        const int par = i == 0 ? -1 : octree_parent(t, mask, P, t.iparent[i], base);
+        r.parent[idx] = par;
+        if (par >= 0) atomicAdd(&r.nchild[par], 1);
+    }
 }
 
 __global__ void emit_leaves_kernel(const uint64_t *__restrict__ k, int64_t n, const float4 *__restrict__ pos,
                                    BinaryTree t, const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
-                                   BHNode *__restrict__ nodes, Records r, SegView sv) {
+                                   BHNode *__restrict__ nodes, Records r, SegView sv, bool parents) {
     const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (b >= n) return;
     const bool lone = !((b > 0 && same_key(k, sv, b, b - 1)) || (b + 1 < n && same_key(k, sv, b, b + 1)));
@@ -501,9 +507,11 @@ __global__ void emit_leaves_kernel(const uint64_t *__restrict__ k, int64_t n, co
     nodes[idx].cm = pos[b];
     nodes[idx].meta = make_int4(__float_as_int(-1.f), static_cast<int>(P[b + 1]), static_cast<int>(b), 1);
     r.level[idx] = kMaxLevel + 1;  // a lone body
-    const int par = n < 2 ? -1 : octree_parent(t, mask, P, t.lparent[b], sv.seg ? 32 : 0);
-    r.parent[idx] = par;
-    if (par >= 0) atomicAdd(&r.nchild[par], 1);
+    if (parents) {
+        const int par = n < 2 ? -1 : octree_parent(t, mask, P, t.lparent[b], sv.seg ? 32 : 0);
+        r.parent[idx] = par;
+        if (par >= 0) atomicAdd(&r.nchild[par], 1);
+    }
 }
 
 // The reference's child order (Octree::getNextNode, src/Octree/Octree.cpp:148-153):
@@ -520,9 +528,12 @@ __device__ __forceinline__ int reference_child_index(uint32_t digit) {
 // own. A cell of the reference's tree that has a single occupied child is
 // skipped here but leaves its trace: (c * m) / m once per skipped level. The
 // reference also keeps lone bodies no shallower than its fixed top levels
-// (depth `father_depth`). The last child to finish computes its parent; a
-// cell all of whose children are leaves is flagged (meta.w = -bodies) so the
-// traversal can sum its bodies directly.
+// (depth `father_depth`). A cell all of whose children are leaves is flagged
+// (meta.w = -bodies) so the traversal can sum its bodies directly. Two
+// schedules give the same bits: the climb (one launch; the last child to
+// arrive at a cell computes it and climbs on) and the level schedule (bucket
+// leaves, then one launch per octree level from the deepest up, no atomics),
+// which is faster from about 2^21 bodies and for ensembles.
 __device__ __forceinline__ float4 round_trips(float4 c, int times) {
     for (int q = 0; q < times; ++q) {
         c.x = __fdiv_rn(__fmul_rn(c.x, c.w), c.w);
@@ -532,9 +543,27 @@ __device__ __forceinline__ float4 round_trips(float4 c, int times) {
     return c;
 }
 
-__global__ void upsweep_kernel(const uint64_t *__restrict__ k, int64_t n, const float4 *__restrict__ pos,
-                               const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
-                               BHNode *__restrict__ nodes, Records r, int father_depth, int *status, SegView sv) {
+// Centre of mass of the bucket (bodies with identical keys) whose first body
+// is b: its occupied bodies in body order, each step rounded on its own.
+__device__ __forceinline__ float4 bucket_cm(const uint64_t *__restrict__ k, int64_t n, const float4 *__restrict__ pos,
+                                            const SegView &sv, int64_t b) {
+    float cx = 0.f, cy = 0.f, cz = 0.f, m = 0.f;
+    for (int64_t q = b; q < n && same_key(k, sv, q, b); ++q) {
+        const float4 o = pos[q];
+        if (!(o.w > 0.f)) continue;
+        cx = __fadd_rn(cx, __fmul_rn(o.x, o.w));
+        cy = __fadd_rn(cy, __fmul_rn(o.y, o.w));
+        cz = __fadd_rn(cz, __fmul_rn(o.z, o.w));
+        m = __fadd_rn(m, o.w);
+    }
+    return m > 0.f ? make_float4(__fdiv_rn(cx, m), __fdiv_rn(cy, m), __fdiv_rn(cz, m), m)
+                   : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void upsweep_climb_kernel(const uint64_t *__restrict__ k, int64_t n, const float4 *__restrict__ pos,
+                                     const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
+                                     BHNode *__restrict__ nodes, Records r, int father_depth, int *status,
+                                     SegView sv) {
     const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (b >= n) return;
     if (sv.seg) father_depth = sv.fdepth[sv.seg[b]];
@@ -546,17 +575,7 @@ __global__ void upsweep_kernel(const uint64_t *__restrict__ k, int64_t n, const 
     } else if (!left_eq) {
         // first body of a bucket: its record is the level-21 cell starting here
         rec = static_cast<int>(P[b] + __popc(mask[b] & ((1u << kMaxLevel) - 1u)));
-        float cx = 0.f, cy = 0.f, cz = 0.f, m = 0.f;
-        for (int64_t q = b; q < n && same_key(k, sv, q, b); ++q) {
-            const float4 o = pos[q];
-            if (!(o.w > 0.f)) continue;
-            cx = __fadd_rn(cx, __fmul_rn(o.x, o.w));
-            cy = __fadd_rn(cy, __fmul_rn(o.y, o.w));
-            cz = __fadd_rn(cz, __fmul_rn(o.z, o.w));
-            m = __fadd_rn(m, o.w);
-        }
-        nodes[rec].cm = m > 0.f ? make_float4(__fdiv_rn(cx, m), __fdiv_rn(cy, m), __fdiv_rn(cz, m), m)
-                                : make_float4(0.f, 0.f, 0.f, 0.f);
+        nodes[rec].cm = bucket_cm(k, n, pos, sv, b);
     } else {
         return;
     }
@@ -610,6 +629,123 @@ __global__ void upsweep_kernel(const uint64_t *__restrict__ k, int64_t n, const 
         rec = par;
     }
     record_error(status, NBODY_ERR_CAPACITY);  // deeper than any octree: broken tree
+}
+
+// Buckets (bodies with identical keys; a level-kMaxLevel leaf): the centre of
+// mass of their occupied bodies, in body order. Lone-body leaves already hold
+// their body.
+__global__ void bucket_cm_kernel(const uint64_t *__restrict__ k, int64_t n, const float4 *__restrict__ pos,
+                                 const uint32_t *__restrict__ mask, const uint32_t *__restrict__ P,
+                                 BHNode *__restrict__ nodes, SegView sv) {
+    const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    const bool left_eq = b > 0 && same_key(k, sv, b, b - 1);
+    const bool right_eq = b + 1 < n && same_key(k, sv, b, b + 1);
+    if (left_eq || !right_eq) return;  // not the first body of a bucket
+    const int rec = static_cast<int>(P[b] + __popc(mask[b] & ((1u << kMaxLevel) - 1u)));
+    nodes[rec].cm = bucket_cm(k, n, pos, sv, b);
+}
+
+// Cells per octree level (levels 0 .. kMaxLevel - 1) over records [0, *total).
+__global__ void level_count_kernel(const int *__restrict__ level, const uint32_t *__restrict__ total,
+                                   unsigned *__restrict__ lvl) {
+    __shared__ unsigned h[kMaxLevel];
+    if (threadIdx.x < kMaxLevel) h[threadIdx.x] = 0u;
+    __syncthreads();
+    const int64_t nrec = *total;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < nrec; r += stride) {
+        const int L = level[r];
+        if (L >= 0 && L < kMaxLevel) atomicAdd(&h[L], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < kMaxLevel && h[threadIdx.x]) atomicAdd(&lvl[threadIdx.x], h[threadIdx.x]);
+}
+
+// Groups the cell records by level into list (one record per thread; the grid
+// covers the record capacity): a block reserves one range per level with a
+// single global atomic, its records take consecutive places in it.
+__global__ void level_scatter_kernel(const int *__restrict__ level, const uint32_t *__restrict__ total,
+                                     unsigned *__restrict__ lvl, unsigned *__restrict__ list, int64_t cap,
+                                     int *status) {
+    __shared__ unsigned h[kMaxLevel], base[kMaxLevel], off[kMaxLevel];
+    if (threadIdx.x == 0) {
+        unsigned run = 0;
+        for (int L = 0; L < kMaxLevel; ++L) {
+            off[L] = run;
+            run += lvl[L];
+        }
+    }
+    if (threadIdx.x < kMaxLevel) h[threadIdx.x] = 0u;
+    __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x < kMaxLevel) lvl[32 + threadIdx.x] = off[threadIdx.x];
+    const int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int L = r < *total ? level[r] : -1;
+    const bool cell = L >= 0 && L < kMaxLevel;
+    const unsigned local = cell ? atomicAdd(&h[L], 1u) : 0u;
+    __syncthreads();
+    if (threadIdx.x < kMaxLevel && h[threadIdx.x])
+        base[threadIdx.x] = off[threadIdx.x] + atomicAdd(&lvl[64 + threadIdx.x], h[threadIdx.x]);
+    __syncthreads();
+    if (!cell) return;
+    const int64_t at = static_cast<int64_t>(base[L]) + local;
+    if (at >= cap) {
+        record_error(status, NBODY_ERR_CAPACITY);
+        return;
+    }
+    list[at] = static_cast<unsigned>(r);
+}
+
+// The cells of one level: each sums its children (already final) in the
+// reference's child order.
+__global__ void level_cm_kernel(int L, const uint64_t *__restrict__ k, int64_t n, BHNode *__restrict__ nodes,
+                                const int *__restrict__ level, const unsigned *__restrict__ list,
+                                const unsigned *__restrict__ lvl, int father_depth, int *status, SegView sv) {
+    const unsigned count = lvl[L], first = lvl[32 + L];
+    const unsigned stride = gridDim.x * blockDim.x;
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += stride) {
+        const int par = static_cast<int>(list[first + q]);
+        const int4 pm = nodes[par].meta;
+        const int fd = sv.seg ? sv.fdepth[sv.seg[pm.z]] : father_depth;
+        float4 slot[8];
+        bool used[8] = {false, false, false, false, false, false, false, false};
+        bool all_leaves = true;
+        int bodies = 0;
+        int c = par + 1;
+        for (int guard = 0; c < pm.y && guard < 8; ++guard) {
+            const int4 cmeta = nodes[c].meta;
+            const float4 cc = nodes[c].cm;
+            const int cl = level[c];
+            const uint32_t digit = static_cast<uint32_t>(k[cmeta.z] >> (63 - 3 * (L + 1))) & 7u;
+            int trips;
+            if (cl >= kMaxLevel) {  // a leaf (lone body or bucket)
+                trips = fd - (L + 1) > 0 ? fd - (L + 1) : 0;
+                bodies += cmeta.w;
+            } else {
+                trips = cl - L - 1;
+                all_leaves = false;
+            }
+            if (cc.w > 0.f) {
+                const int j = reference_child_index(digit);
+                slot[j] = round_trips(cc, trips);
+                used[j] = true;
+            }
+            c = cmeta.y;
+        }
+        if (c != pm.y) record_error(status, NBODY_ERR_CAPACITY);  // more than 8 children: broken tree
+        float cx = 0.f, cy = 0.f, cz = 0.f, m = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (!used[j]) continue;
+            cx = __fadd_rn(cx, __fmul_rn(slot[j].x, slot[j].w));
+            cy = __fadd_rn(cy, __fmul_rn(slot[j].y, slot[j].w));
+            cz = __fadd_rn(cz, __fmul_rn(slot[j].z, slot[j].w));
+            m = __fadd_rn(m, slot[j].w);
+        }
+        nodes[par].cm = m > 0.f ? make_float4(__fdiv_rn(cx, m), __fdiv_rn(cy, m), __fdiv_rn(cz, m), m)
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (all_leaves) nodes[par].meta.w = -bodies;
+    }
 }
 
 // --------------------------------------------------------------- traversal
@@ -1122,6 +1258,8 @@ size_t bh_workspace_layout(int64_t n, void *base, BHWorkspace *w) {
     w->rec.parent = static_cast<int *>(take(sizeof(int) * 2 * nn));
     w->rec.nchild = static_cast<int *>(take(sizeof(int) * 2 * nn));
     w->rec.arrive = static_cast<unsigned *>(take(sizeof(unsigned) * 2 * nn));
+    w->rec.list = w->rec.arrive;  // one schedule or the other per build
+    w->rec.lvl = static_cast<unsigned *>(take(sizeof(unsigned) * 96));
     w->mask = static_cast<uint32_t *>(take(sizeof(uint32_t) * nn));
     w->cnt = static_cast<uint32_t *>(take(sizeof(uint32_t) * nn));
     w->P = static_cast<uint32_t *>(take(sizeof(uint32_t) * (nn + 1)));
@@ -1191,18 +1329,44 @@ cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaSt
     scan_tiles_kernel<<<tiles, kScanThreads, 0, st>>>(w.cnt, n, w.P, w.scan_sums);
     scan_sums_kernel<<<1, 1024, 0, st>>>(w.scan_sums, tiles, w.P + n);
     scan_add_kernel<<<grid_for(n, 256), 256, 0, st>>>(w.P, n, w.scan_sums);
-    const size_t nrec = 2 * static_cast<size_t>(n > 1 ? n : 2);
-    e = cudaMemsetAsync(w.rec.nchild, 0, sizeof(int) * nrec, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(w.rec.arrive, 0, sizeof(unsigned) * nrec, st);
-    if (e != cudaSuccess) return e;
+    // Upsweep schedule (same bits either way): the climb below 2^21 bodies of
+    // one system, where one launch beats one per level; NBODY_UPSWEEP =
+    // "climb" or "levels" forces one.
+    bool levels = sv.seg != nullptr || n >= (int64_t(1) << 21);
+    if (const char *env = std::getenv("NBODY_UPSWEEP")) {
+        if (std::strcmp(env, "climb") == 0) levels = false;
+        if (std::strcmp(env, "levels") == 0) levels = true;
+    }
+    // Records: at most 2n (n - 1 cells and n leaves).
+    const int64_t cap = 2 * (n > 1 ? n : 2);
+    if (!levels) {
+        e = cudaMemsetAsync(w.rec.nchild, 0, sizeof(int) * static_cast<size_t>(cap), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(w.rec.arrive, 0, sizeof(unsigned) * static_cast<size_t>(cap), st);
+        if (e != cudaSuccess) return e;
+    }
     if (n >= 2)
         emit_cells_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(k, n, w.tree, w.mask, w.P, w.box, w.nodes, w.rec,
-                                                                sv);
-    emit_leaves_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.tree, w.mask, w.P, w.nodes, w.rec, sv);
+                                                                sv, !levels);
+    emit_leaves_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.tree, w.mask, w.P, w.nodes, w.rec, sv,
+                                                         !levels);
     if (timer) timer->end(kStageBuild, st);
     if (timer) timer->begin(kStageUpsweep, st);
-    upsweep_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.mask, w.P, w.nodes, w.rec,
-                                                     father_depth(n), status, sv);
+    if (!levels) {
+        upsweep_climb_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.mask, w.P, w.nodes, w.rec,
+                                                               father_depth(n), status, sv);
+        if (timer) timer->end(kStageUpsweep, st);
+        return cudaGetLastError();
+    }
+    e = cudaMemsetAsync(w.rec.lvl, 0, sizeof(unsigned) * 96, st);
+    if (e != cudaSuccess) return e;
+    bucket_cm_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.mask, w.P, w.nodes, sv);
+    const unsigned spread = static_cast<unsigned>(std::min<int64_t>(grid_for(n, 256), 1216));
+    level_count_kernel<<<spread, 256, 0, st>>>(w.rec.level, w.P + n, w.rec.lvl);
+    level_scatter_kernel<<<grid_for(cap, 256), 256, 0, st>>>(w.rec.level, w.P + n, w.rec.lvl, w.rec.list, cap,
+                                                             status);
+    const int fd = father_depth(n);
+    for (int L = kMaxLevel - 1; L >= 0; --L)
+        level_cm_kernel<<<spread, 256, 0, st>>>(L, k, n, w.nodes, w.rec.level, w.rec.list, w.rec.lvl, fd, status, sv);
     if (timer) timer->end(kStageUpsweep, st);
     return cudaGetLastError();
 }

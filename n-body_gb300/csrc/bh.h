@@ -27,11 +27,17 @@ struct BinaryTree {
     int *lo, *hi, *left, *right, *delta, *iparent, *lparent, *top;
 };
 
-// Per-record bookkeeping for the bottom-up pass: cell level (kMaxLevel + 1
-// for a lone body), octree parent record, child count, arrivals.
+// Per-record bookkeeping for the bottom-up pass: level[r] = octree level of
+// record r (kMaxLevel for a bucket, kMaxLevel + 1 for a lone body). The
+// climbing schedule uses parent (octree parent record), nchild and arrive;
+// the level schedule uses list (the cell records grouped by level; it shares
+// arrive's storage) and lvl: lvl[0..32) = cells per level, lvl[32..64) = where
+// each level's group starts in list, lvl[64..96) = fill cursors.
 struct Records {
     int *level, *parent, *nchild;
     unsigned *arrive;
+    unsigned *list;
+    unsigned *lvl;
 };
 
 // Systems packed back to back (an ensemble): seg[b] = system of body b,

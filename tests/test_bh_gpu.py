@@ -202,6 +202,38 @@ def test_tree_invariants(nb, cuda, oracle, kind):
         assert s2[i] == reference_cell_side2(keys[body], level, box), (i, level)
 
 
+@pytest.mark.parametrize("kind", ["plummer", "duplicates"])
+def test_upsweep_schedules_agree(nb, cuda, monkeypatch, kind):
+    """The climbing upsweep (one launch, atomic arrivals) and the level schedule
+    (one launch per octree level) build the same records bit for bit, buckets
+    of identical positions included, and so the same forces and steps."""
+    torch = cuda
+    from nbody_gb300 import initializers as I
+
+    n = 50_000
+    if kind == "plummer":
+        pos, vel, mass = I.plummer(n, seed=43)
+    else:
+        pos, vel, mass = I.uniform_ball(n, seed=44)
+        pos[2000:2100] = pos[2000]
+        pos[7:9] = pos[6]
+    out = {}
+    for sched in ("climb", "levels"):
+        monkeypatch.setenv("NBODY_UPSWEEP", sched)
+        f, s = bh_forces(nb, torch, pos, mass)
+        out[sched] = (f, *s.bh_tree())
+        s.close()
+        sysm = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+        s = solver_for(nb, n)
+        s.update_particle_positions(sysm, steps=2)
+        s.close()
+        out[sched + " steps"] = (sysm.positions, sysm.velocities, sysm.accelerations)
+    for a, b in zip(out["climb"], out["levels"]):
+        np.testing.assert_array_equal(a, b)
+    for a, b in zip(out["climb steps"], out["levels steps"]):
+        np.testing.assert_array_equal(a, b)
+
+
 # ---------------------------------------------------------------------- forces
 @pytest.mark.parametrize("name", BH_FIXTURES)
 def test_bh_forces_match_reference_golden(nb, cuda, oracle, name):
