@@ -1314,6 +1314,20 @@ cudaError_t bh_gather(int64_t n, const BHWorkspace &w, const float4 *pos_in, con
     return cudaGetLastError();
 }
 
+bool bh_upsweep_by_levels(int64_t n, bool ensemble) {
+    // Same bits either way: the climb below 2^21 bodies of one system, where
+    // one launch beats one per level; NBODY_UPSWEEP = "climb" or "levels"
+    // forces one.
+    bool levels = ensemble || n >= (int64_t(1) << 21);
+    if (const char *env = std::getenv("NBODY_UPSWEEP")) {
+        if (std::strcmp(env, "climb") == 0) levels = false;
+        if (std::strcmp(env, "levels") == 0) levels = true;
+    }
+    return levels;
+}
+
+int bh_upsweep_launches(int64_t n, bool ensemble) { return bh_upsweep_by_levels(n, ensemble) ? 3 + kMaxLevel : 1; }
+
 cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaStream_t st, int *status,
                      StageTimer *timer, const SegView &sv) {
     if (timer) timer->begin(kStageBuild, st);
@@ -1329,14 +1343,7 @@ cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaSt
     scan_tiles_kernel<<<tiles, kScanThreads, 0, st>>>(w.cnt, n, w.P, w.scan_sums);
     scan_sums_kernel<<<1, 1024, 0, st>>>(w.scan_sums, tiles, w.P + n);
     scan_add_kernel<<<grid_for(n, 256), 256, 0, st>>>(w.P, n, w.scan_sums);
-    // Upsweep schedule (same bits either way): the climb below 2^21 bodies of
-    // one system, where one launch beats one per level; NBODY_UPSWEEP =
-    // "climb" or "levels" forces one.
-    bool levels = sv.seg != nullptr || n >= (int64_t(1) << 21);
-    if (const char *env = std::getenv("NBODY_UPSWEEP")) {
-        if (std::strcmp(env, "climb") == 0) levels = false;
-        if (std::strcmp(env, "levels") == 0) levels = true;
-    }
+    const bool levels = bh_upsweep_by_levels(n, sv.seg != nullptr);
     // Records: at most 2n (n - 1 cells and n leaves).
     const int64_t cap = 2 * (n > 1 ? n : 2);
     if (!levels) {

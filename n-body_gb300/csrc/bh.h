@@ -85,6 +85,11 @@ cudaError_t bh_sort(int64_t n, BHWorkspace &w, cudaStream_t st, int *status, Sta
 cudaError_t bh_gather(int64_t n, const BHWorkspace &w, const float4 *pos_in, const float4 *vel_in,
                       const float4 *acc_in, const int *id_in, float4 *pos_out, float4 *vel_out, float4 *acc_out,
                       int *id_out, cudaStream_t st, int *status, StageTimer *timer);
+// Upsweep schedule of bh_build: true = one launch per octree level (ensembles,
+// and systems from 2^21 bodies), false = the single-launch climb; and the
+// kernel launches it takes.
+bool bh_upsweep_by_levels(int64_t n, bool ensemble);
+int bh_upsweep_launches(int64_t n, bool ensemble);
 cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaStream_t st, int *status,
                      StageTimer *timer, const SegView &sv = SegView{});
 // Forces for every sorted body; with pos_out set, also the reference
