@@ -93,18 +93,20 @@ int fail(nbody_ctx *ctx, cudaError_t e) {
 
 bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
-// The device-mapped address of a page-locked host buffer (cudaHostAlloc /
-// cudaMallocHost, or cudaHostRegister'ed and mapped), or nullptr for any other
-// pointer: pageable memory, device memory, or an address not 16-byte aligned.
+// The address, on `device`, of a page-locked host buffer (cudaHostAlloc /
+// cudaMallocHost, or cudaHostRegister'ed and mapped) registered with that
+// device, or nullptr for any other pointer: pageable memory, device memory,
+// another device's page-locked memory, or an address not 16-byte aligned.
 // Only such addresses are handed to the host_gather / host_scatter kernels.
-float4 *mapped(const void *p) {
+float4 *mapped(const void *p, int device) {
     if (!p || !aligned16(p)) return nullptr;
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    if (a.type != cudaMemoryTypeHost || !a.devicePointer || !aligned16(a.devicePointer)) return nullptr;
+    if (a.type != cudaMemoryTypeHost || a.device != device || !a.devicePointer || !aligned16(a.devicePointer))
+        return nullptr;
     return static_cast<float4 *>(a.devicePointer);
 }
 
@@ -348,9 +350,9 @@ int nbody_upload(nbody_ctx *ctx, const float *positions4, const float *velocitie
     const size_t b4 = static_cast<size_t>(ctx->n) * sizeof(float4);
     // Page-locked host buffers are read in place by one kernel; otherwise one
     // copy per array into the staging area, then the pack kernel.
-    const float4 *mp = mapped(positions4), *mm = mapped(masses4);
-    const float4 *mv = velocities4 ? mapped(velocities4) : nullptr;
-    const float4 *ma = accelerations4 ? mapped(accelerations4) : nullptr;
+    const float4 *mp = mapped(positions4, ctx->device), *mm = mapped(masses4, ctx->device);
+    const float4 *mv = velocities4 ? mapped(velocities4, ctx->device) : nullptr;
+    const float4 *ma = accelerations4 ? mapped(accelerations4, ctx->device) : nullptr;
     if (mp && mm && (!velocities4 || mv) && (!accelerations4 || ma)) {
         NB_CK(ctx, nbody::host_gather(mp, mm, mv, ma, ctx->pos[0], ctx->vel, ctx->acc, ctx->n, ctx->stream));
     } else {
@@ -392,8 +394,11 @@ int nbody_download(nbody_ctx *ctx, float *positions4, float *velocities4, float 
         // Page-locked host buffers are written in place by one kernel, in the
         // caller's order (through the inverse of the sorted order, built in the
         // staging area, when the state is sorted).
-        float4 *mp = positions4 ? mapped(positions4) : nullptr, *mv = velocities4 ? mapped(velocities4) : nullptr;
-        float4 *ma = accelerations4 ? mapped(accelerations4) : nullptr, *mf = forces4 ? mapped(forces4) : nullptr;
+        const int dev = ctx->device;
+        float4 *mp = positions4 ? mapped(positions4, dev) : nullptr;
+        float4 *mv = velocities4 ? mapped(velocities4, dev) : nullptr;
+        float4 *ma = accelerations4 ? mapped(accelerations4, dev) : nullptr;
+        float4 *mf = forces4 ? mapped(forces4, dev) : nullptr;
         if ((!positions4 || mp) && (!velocities4 || mv) && (!accelerations4 || ma) && (!forces4 || mf)) {
             const bool bh = ctx->mode == NBODY_MODE_BH;
             const int *ids = (bh && ctx->ids_valid) ? ctx->ids[ctx->bh_va] : nullptr;
