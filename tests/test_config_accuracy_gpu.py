@@ -3,7 +3,10 @@ sizes (a sample of bodies), and for the discs also against the -v 6 port
 (oracle/nbody_oracle.c, patched capacities) at a reduced size: the Barnes-Hut
 error is the method's when the GPU's FP64 error matches the port's.
 
-  config 1, direct sum, N = 16,384 ball:          RMS <= 1e-5 (the accuracy gate)
+  config 1, direct sum, N = 16,384 ball:          RMS <= 1e-5 (the accuracy gate); after the
+                                                   config's 100 steps, positions within 1e-4 of
+                                                   the -v 2 port and no farther than the port
+                                                   from an FP64 run
   config 2, Barnes-Hut theta = 0.5, N = 2^20:     RMS <= 1.2e-3 (gate 1e-3 at theta = 0.5;
                                                    measured 9.7e-4)
   config 3, Barnes-Hut theta = 0.6, N = 2^24 discs: RMS 1.4e-2, the method's at this theta:
@@ -51,6 +54,49 @@ def test_config1_direct_sum_vs_fp64(nb, cuda, oracle):
     rms, mx = _rel(a, oracle.direct_f64(p, m, 40.0))
     print(f"config 1 vs FP64: RMS {rms:.3g}, max {mx:.3g}")
     assert rms <= 1e-5 and mx <= 1e-4, (rms, mx)
+
+
+def test_config1_hundred_steps_vs_port_and_fp64(nb, cuda, oracle):
+    """Config 1 in full: 100 steps of the 16,384-body ball. The final state is
+    compared with the -v 2 port's 100 steps (FP32, same integrator) and with an
+    FP64 run (FP64 direct-sum forces at the pre-step positions, the reference
+    integrator in FP64). Bounds: GPU vs port, positions within 1e-4 (13 FP32
+    ulps at the ball's radius) and final forces RMS <= 1e-5; GPU vs FP64,
+    positions within 1e-3, and no farther than the port is from FP64."""
+    from nbody_gb300 import initializers as I
+
+    n, dt, eps2, steps = 16384, 0.0035, 40.0, 100
+    pos, vel, mass = I.uniform_ball(n, seed=12345)
+    s = nb.ParticleSolverCUDA(dt, eps2, n, mode="pp")
+    s.upload(nb.ParticleSystem(pos.copy(), vel.copy(), mass))
+    s.step(steps)
+    z = np.zeros((n, 4), np.float32)
+    gpu = nb.ParticleSystem(z.copy(), z.copy(), mass, z.copy())
+    s.download(gpu)
+    s.close()
+    pk, vk, ak, fk, _ = oracle.pp_run(pos, vel, np.zeros_like(pos), mass, dt, eps2, steps)
+
+    x = pos[:, :3].astype(np.float64)
+    v = vel[:, :3].astype(np.float64)
+    a = np.zeros_like(x)
+    h = dt / 2
+    p4 = np.zeros((n, 4), np.float32)
+    for _ in range(steps):
+        p4[:, :3] = x
+        f = oracle.direct_f64(p4, mass, eps2)
+        v += a * h
+        x += v * dt
+        a = f
+        v += a * h
+
+    d_port = float(np.abs(gpu.positions[:, :3].astype(np.float64) - pk[:, :3]).max())
+    rms_f, _ = _rel(gpu.accelerations, fk)
+    e_gpu = float(np.abs(gpu.positions[:, :3].astype(np.float64) - x).max())
+    e_port = float(np.abs(pk[:, :3].astype(np.float64) - x).max())
+    print(f"config 1, 100 steps: |x_gpu - x_port| max {d_port:.3g}, forces RMS {rms_f:.3g}; "
+          f"vs FP64 max |dx| GPU {e_gpu:.3g}, port {e_port:.3g}")
+    assert d_port <= 1e-4 and rms_f <= 1e-5, (d_port, rms_f)
+    assert e_gpu <= 1e-3 and e_gpu <= 1.5 * e_port + 1e-5, (e_gpu, e_port)
 
 
 def test_config2_barnes_hut_1m_vs_fp64(nb, cuda, oracle):
