@@ -8,7 +8,8 @@ error is the method's when the GPU's FP64 error matches the port's.
                                                    the -v 2 port and no farther than the port
                                                    from an FP64 run
   config 2, Barnes-Hut theta = 0.5, N = 2^20:     RMS <= 1.2e-3 (gate 1e-3 at theta = 0.5;
-                                                   measured 9.7e-4)
+                                                   measured 9.7e-4); after the config's 10 steps,
+                                                   forces and positions against the -v 6 port
   config 3, Barnes-Hut theta = 0.6, N = 2^24 discs: RMS 1.4e-2, the method's at this theta:
                                                    a one-off run of the port on the same
                                                    2^24 bodies gave the same FP64 error
@@ -108,6 +109,37 @@ def test_config2_barnes_hut_1m_vs_fp64(nb, cuda, oracle):
     rms, mx = _rel(a[idx], oracle.direct_f64(p, m, 40.0, idx=idx))
     print(f"config 2 vs FP64 (1,024 bodies): RMS {rms:.3g}, max {mx:.3g}")
     assert rms <= 1.2e-3, (rms, mx)
+
+
+def test_config2_ten_steps_vs_port(nb, cuda, oracle):
+    """Config 2 in full: 10 steps of the 2^20-body Plummer sphere against the
+    -v 6 port (patched capacities; the reference's fixed regions overflow on this
+    input). Same cells, sides and opening test; centres of mass are summed in
+    another order, so a few opening decisions flip and move a body's force by
+    about one cell's Barnes-Hut error. Bounds on the last step's forces: RMS <=
+    3e-5, 99.9th percentile <= 5e-4, worst <= 2e-3; positions within 1e-6 of the
+    sphere's extent."""
+    from nbody_gb300 import initializers as I
+
+    n, steps = 1 << 20, 10
+    pos, vel, mass = I.plummer(n, a=100.0, seed=12345)
+    sysm = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+    s = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="bh", theta2=0.25)
+    s.update_particle_positions(sysm, steps=steps)
+    s.close()
+    pk, vk, ak, fk, info = oracle.bh_run(pos, vel, np.zeros_like(pos), mass, 0.0035, 40.0, steps, theta2=0.25,
+                                         patched=True)
+    assert info["rc"] == 0
+    g = np.asarray(sysm.forces, np.float64)[:, :3]
+    r = np.asarray(fk, np.float64)[:, :3]
+    e = np.linalg.norm(g - r, axis=1) / np.linalg.norm(r, axis=1)
+    rms, p999 = float(np.sqrt(np.mean(e * e))), float(np.percentile(e, 99.9))
+    dx = float(np.abs(sysm.positions[:, :3].astype(np.float64) - pk[:, :3]).max())
+    scale = float(np.abs(pk[:, :3]).max())
+    print(f"config 2, 10 steps vs port: forces RMS {rms:.3g}, p99.9 {p999:.3g}, max {e.max():.3g}; "
+          f"max |dx| {dx:.3g} of extent {scale:.4g}")
+    assert rms <= 3e-5 and p999 <= 5e-4 and e.max() <= 2e-3, (rms, p999, e.max())
+    assert dx <= 1e-6 * scale, (dx, scale)
 
 
 def test_config3_discs_error_is_the_methods(nb, cuda, oracle):
