@@ -89,10 +89,14 @@ def tune(device: int = 0, grid=GRID, bodies: int = 2_000_000, verbose: bool = Fa
             table[n] = 1e9 * t / (copies * n)
         if verbose:
             print(f"N={n}: pp {ns_pp[n]:.3f} ns, bh {ns_bh[n]:.3f} ns per body-step", flush=True)
+    # The crossover comes from the timings as stored (rounded), so that the file
+    # reproduces it.
+    ns_pp = {k: round(v, 4) for k, v in ns_pp.items()}
+    ns_bh = {k: round(v, 4) for k, v in ns_bh.items()}
     crossover = crossover_from(grid, ns_pp, ns_bh)
     return {"version": VERSION, "device_name": _device_name(device), "crossover": int(crossover), "pp_shape": best,
-            "ns_per_body_step": {"pp": {str(k): round(v, 4) for k, v in ns_pp.items()},
-                                 "bh": {str(k): round(v, 4) for k, v in ns_bh.items()}},
+            "ns_per_body_step": {"pp": {str(k): v for k, v in ns_pp.items()},
+                                 "bh": {str(k): v for k, v in ns_bh.items()}},
             "pp_shape_ms_per_step": {k: round(v * 1e3, 4) for k, v in shapes.items()},
             "tuned_at": time.strftime("%Y-%m-%dT%H:%M:%S")}
 
