@@ -135,32 +135,7 @@ __global__ void __launch_bounds__(T, pp_min_blocks<K>())
         const int64_t jt = j0 + static_cast<int64_t>(t) * kPPTile;
         const int cnt = static_cast<int>((j1 - jt) < kPPTile ? (j1 - jt) : kPPTile);
         const int npr = (cnt + 1) >> 1;
-        const float4 *pr = pairs[t & 1];
-#pragma unroll 2
-        for (int q = 0; q < npr; ++q) {
-            const float4 u = pr[2 * q];
-            const float4 v = pr[2 * q + 1];
-            const float2 xj = f2(u.x, u.y), yj = f2(u.z, u.w), zj = f2(v.x, v.y), mj = f2(v.z, v.w);
-#pragma unroll
-            for (int r = 0; r < K; ++r) {
-                const float2 dx = __fadd2_rn(xj, nx[r]);
-                const float2 dy = __fadd2_rn(yj, ny[r]);
-                const float2 dz = __fadd2_rn(zj, nz[r]);
-                float2 r2 = __ffma2_rn(dx, dx, e2);
-                r2 = __ffma2_rn(dy, dy, r2);
-                r2 = __ffma2_rn(dz, dz, r2);
-                float2 inv = f2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
-                if (GUARD) {
-                    inv.x = r2.x > 0.f ? inv.x : 0.f;
-                    inv.y = r2.y > 0.f ? inv.y : 0.f;
-                }
-                const float2 inv2 = __fmul2_rn(inv, inv);
-                const float2 s = __fmul2_rn(__fmul2_rn(mj, inv), inv2);
-                ax[r] = __ffma2_rn(dx, s, ax[r]);
-                ay[r] = __ffma2_rn(dy, s, ay[r]);
-                az[r] = __ffma2_rn(dz, s, az[r]);
-            }
-        }
+        pair_forces<K, GUARD>(pairs[t & 1], npr, nx, ny, nz, e2, ax, ay, az);
         if (!__syncthreads_and(ok)) {  // also: every thread is done with pairs[t & 1]
             failed = true;
             fail_at = t + 1;

@@ -50,6 +50,42 @@ __device__ __forceinline__ void integrate_body(int64_t i, float4 p, float fx, fl
     if (g.force) g.force[i] = anew;
 }
 
+// The inner loop: forces on this thread's K i-bodies from npr j-pairs laid out
+// {x0 x1 y0 y1}{z0 z1 m0 m1}, two interactions per packed f32x2 instruction
+// (12 FADD2/FFMA2/FMUL2 + 2 MUFU.RSQ per pair of interactions). nx/ny/nz hold
+// the negated i-positions duplicated in both halves. GUARD drops pairs at zero
+// distance (needed when eps2 == 0).
+template <int K, bool GUARD>
+__device__ __forceinline__ void pair_forces(const float4 *__restrict__ pr, int npr, const float2 (&nx)[K],
+                                            const float2 (&ny)[K], const float2 (&nz)[K], float2 e2,
+                                            float2 (&ax)[K], float2 (&ay)[K], float2 (&az)[K]) {
+#pragma unroll 2
+    for (int q = 0; q < npr; ++q) {
+        const float4 u = pr[2 * q];
+        const float4 v = pr[2 * q + 1];
+        const float2 xj = f2(u.x, u.y), yj = f2(u.z, u.w), zj = f2(v.x, v.y), mj = f2(v.z, v.w);
+#pragma unroll
+        for (int r = 0; r < K; ++r) {
+            const float2 dx = __fadd2_rn(xj, nx[r]);
+            const float2 dy = __fadd2_rn(yj, ny[r]);
+            const float2 dz = __fadd2_rn(zj, nz[r]);
+            float2 r2 = __ffma2_rn(dx, dx, e2);
+            r2 = __ffma2_rn(dy, dy, r2);
+            r2 = __ffma2_rn(dz, dz, r2);
+            float2 inv = f2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+            if (GUARD) {
+                inv.x = r2.x > 0.f ? inv.x : 0.f;
+                inv.y = r2.y > 0.f ? inv.y : 0.f;
+            }
+            const float2 inv2 = __fmul2_rn(inv, inv);
+            const float2 s = __fmul2_rn(__fmul2_rn(mj, inv), inv2);
+            ax[r] = __ffma2_rn(dx, s, ax[r]);
+            ay[r] = __ffma2_rn(dy, s, ay[r]);
+            az[r] = __ffma2_rn(dz, s, az[r]);
+        }
+    }
+}
+
 // Shared-memory staging of one CTA: the TMA landing ring and the j-pair tile.
 struct Ring {
     float4 (*tile)[kPPTile];
@@ -105,32 +141,7 @@ __device__ bool item_forces(const float4 *__restrict__ pos, int64_t j0, int64_t 
         }
         __syncthreads();
         if (tid == 0 && t + kPPStages < ntiles) issue(t + kPPStages);
-        const float4 *pr = ring.pairs;
-#pragma unroll 2
-        for (int q = 0; q < npr; ++q) {
-            const float4 u = pr[2 * q];
-            const float4 v = pr[2 * q + 1];
-            const float2 xj = f2(u.x, u.y), yj = f2(u.z, u.w), zj = f2(v.x, v.y), mj = f2(v.z, v.w);
-#pragma unroll
-            for (int r = 0; r < K; ++r) {
-                const float2 dx = __fadd2_rn(xj, nx[r]);
-                const float2 dy = __fadd2_rn(yj, ny[r]);
-                const float2 dz = __fadd2_rn(zj, nz[r]);
-                float2 r2 = __ffma2_rn(dx, dx, e2);
-                r2 = __ffma2_rn(dy, dy, r2);
-                r2 = __ffma2_rn(dz, dz, r2);
-                float2 inv = f2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
-                if (GUARD) {
-                    inv.x = r2.x > 0.f ? inv.x : 0.f;
-                    inv.y = r2.y > 0.f ? inv.y : 0.f;
-                }
-                const float2 inv2 = __fmul2_rn(inv, inv);
-                const float2 s = __fmul2_rn(__fmul2_rn(mj, inv), inv2);
-                ax[r] = __ffma2_rn(dx, s, ax[r]);
-                ay[r] = __ffma2_rn(dy, s, ay[r]);
-                az[r] = __ffma2_rn(dz, s, az[r]);
-            }
-        }
+        pair_forces<K, GUARD>(ring.pairs, npr, nx, ny, nz, e2, ax, ay, az);
     }
     gt += static_cast<uint32_t>(ntiles);
     return true;
