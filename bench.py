@@ -1,6 +1,7 @@
 """Benchmark of the per-step gravity solve on GB300; prints ONE JSON line.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload bh|discs|pp|ensemble] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload bh|discs|pp|ensemble|serving]
+                    [--impl ours|reference]
 
 Workloads (seeded synthetic inputs with the shapes the configurations name;
 no public dataset is involved):
@@ -35,7 +36,8 @@ A "step" is one ParticleSolver::updateParticlePositions: forces + integrator.
 value: K steps on HBM-resident state, timed with CUDA events on the launch
 stream, L2 flushed (a 256 MiB write) between steps outside the event pair.
 e2e:   the same steps through the C ABI's host-layout call (nbody_update_host)
-with pinned host buffers, every step copying the reference layout in and out.
+with pinned host buffers, every step moving the reference layout in and out
+(the library reads and writes page-locked buffers in place over the host link).
 Multi-GPU: the path is replicated, not sharded ("replicas only"): under
 torchrun every rank steps its own copy and value sums the ranks' work.
 
