@@ -104,7 +104,10 @@ float nbody_get_squared_softening(const nbody_ctx *ctx);
 int nbody_update_host(nbody_ctx *ctx, float *positions4, float *velocities4, float *accelerations4,
                       const float *masses4, float *forces4, int steps);
 
-/* Resident mode: state stays in HBM between calls. */
+/* Resident mode: state stays in HBM between calls. nbody_upload orders its
+ * reads of the host arrays on the context's stream: pageable arrays may be
+ * reused when it returns, page-locked ones only after the next nbody_sync,
+ * nbody_download or nbody_update_host (as with cudaMemcpyAsync). */
 int nbody_upload(nbody_ctx *ctx, const float *positions4, const float *velocities4,
                  const float *accelerations4, const float *masses4);
 int nbody_step(nbody_ctx *ctx, int steps);
