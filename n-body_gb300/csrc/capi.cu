@@ -93,23 +93,6 @@ int fail(nbody_ctx *ctx, cudaError_t e) {
 
 bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
-// The address, on `device`, of a page-locked host buffer (cudaHostAlloc /
-// cudaMallocHost, or cudaHostRegister'ed and mapped) registered with that
-// device, or nullptr for any other pointer: pageable memory, device memory,
-// another device's page-locked memory, or an address not 16-byte aligned.
-// Only such addresses are handed to the host_gather / host_scatter kernels.
-float4 *mapped(const void *p, int device) {
-    if (!p || !aligned16(p)) return nullptr;
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
-    }
-    if (a.type != cudaMemoryTypeHost || a.device != device || !a.devicePointer || !aligned16(a.devicePointer))
-        return nullptr;
-    return static_cast<float4 *>(a.devicePointer);
-}
-
 int ensure_scratch(nbody_ctx *ctx, size_t bytes) {
     if (bytes <= ctx->scratch_bytes) return NBODY_OK;
     if (ctx->scratch) {
@@ -350,9 +333,9 @@ int nbody_upload(nbody_ctx *ctx, const float *positions4, const float *velocitie
     const size_t b4 = static_cast<size_t>(ctx->n) * sizeof(float4);
     // Page-locked host buffers are read in place by one kernel; otherwise one
     // copy per array into the staging area, then the pack kernel.
-    const float4 *mp = mapped(positions4, ctx->device), *mm = mapped(masses4, ctx->device);
-    const float4 *mv = velocities4 ? mapped(velocities4, ctx->device) : nullptr;
-    const float4 *ma = accelerations4 ? mapped(accelerations4, ctx->device) : nullptr;
+    const float4 *mp = nbody::host_mapped(positions4, ctx->device), *mm = nbody::host_mapped(masses4, ctx->device);
+    const float4 *mv = velocities4 ? nbody::host_mapped(velocities4, ctx->device) : nullptr;
+    const float4 *ma = accelerations4 ? nbody::host_mapped(accelerations4, ctx->device) : nullptr;
     if (mp && mm && (!velocities4 || mv) && (!accelerations4 || ma)) {
         NB_CK(ctx, nbody::host_gather(mp, mm, mv, ma, ctx->pos[0], ctx->vel, ctx->acc, ctx->n, ctx->stream));
     } else {
@@ -395,10 +378,10 @@ int nbody_download(nbody_ctx *ctx, float *positions4, float *velocities4, float 
         // caller's order (through the inverse of the sorted order, built in the
         // staging area, when the state is sorted).
         const int dev = ctx->device;
-        float4 *mp = positions4 ? mapped(positions4, dev) : nullptr;
-        float4 *mv = velocities4 ? mapped(velocities4, dev) : nullptr;
-        float4 *ma = accelerations4 ? mapped(accelerations4, dev) : nullptr;
-        float4 *mf = forces4 ? mapped(forces4, dev) : nullptr;
+        float4 *mp = positions4 ? nbody::host_mapped(positions4, dev) : nullptr;
+        float4 *mv = velocities4 ? nbody::host_mapped(velocities4, dev) : nullptr;
+        float4 *ma = accelerations4 ? nbody::host_mapped(accelerations4, dev) : nullptr;
+        float4 *mf = forces4 ? nbody::host_mapped(forces4, dev) : nullptr;
         if ((!positions4 || mp) && (!velocities4 || mv) && (!accelerations4 || ma) && (!forces4 || mf)) {
             const bool bh = ctx->mode == NBODY_MODE_BH;
             const int *ids = (bh && ctx->ids_valid) ? ctx->ids[ctx->bh_va] : nullptr;
@@ -406,8 +389,8 @@ int nbody_download(nbody_ctx *ctx, float *positions4, float *velocities4, float 
                 NB_CK(ctx, nbody::host_scatter(bh ? ctx->pos[ctx->bh_pos] : ctx->pos[ctx->cur],
                                                bh ? ctx->vel2[ctx->bh_va] : ctx->vel,
                                                bh ? ctx->acc2[ctx->bh_va] : ctx->acc, ids,
-                                               reinterpret_cast<int *>(ctx->stage), mp, mv, ma, mf, n, ctx->stream,
-                                               ctx->status));
+                                               reinterpret_cast<int *>(ctx->stage), mp, mv, ma, mf, nullptr, n,
+                                               ctx->stream, ctx->status));
             return read_status(ctx);
         }
     }

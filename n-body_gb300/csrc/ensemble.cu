@@ -614,17 +614,26 @@ int nbody_ensemble_upload(nbody_ensemble *e, int system, const float *positions4
     if ((rc = relayout(e)) != NBODY_OK) return rc;
     Sys &s = e->sys[system];
     const size_t nb = static_cast<size_t>(s.n) * sizeof(float4);
-    EN_CK(e, cudaMemcpyAsync(e->stage, positions4, nb, cudaMemcpyHostToDevice, e->stream));
-    EN_CK(e, cudaMemcpyAsync(e->stage + s.n, masses4, nb, cudaMemcpyHostToDevice, e->stream));
     const bool pp = s.mode == NBODY_MODE_PP;
     float4 *pos = pp ? e->pp_pos[e->pp_cur] + s.first : e->bh_pos[0] + s.first;
     float4 *vel = pp ? e->pp_vel + s.first : e->bh_vel[e->bh_va] + s.first;
     float4 *acc = pp ? e->pp_acc + s.first : e->bh_acc[e->bh_va] + s.first;
-    EN_CK(e, nbody::pack_state(e->stage, e->stage + s.n, pos, s.n, e->stream));
-    if (velocities4) EN_CK(e, cudaMemcpyAsync(vel, velocities4, nb, cudaMemcpyHostToDevice, e->stream));
-    else EN_CK(e, cudaMemsetAsync(vel, 0, nb, e->stream));
-    if (accelerations4) EN_CK(e, cudaMemcpyAsync(acc, accelerations4, nb, cudaMemcpyHostToDevice, e->stream));
-    else EN_CK(e, cudaMemsetAsync(acc, 0, nb, e->stream));
+    // Page-locked host arrays are read in place by one kernel; otherwise one
+    // copy per array into the staging area, then the pack kernel.
+    const float4 *mp = nbody::host_mapped(positions4, e->device), *mm = nbody::host_mapped(masses4, e->device);
+    const float4 *mv = velocities4 ? nbody::host_mapped(velocities4, e->device) : nullptr;
+    const float4 *ma = accelerations4 ? nbody::host_mapped(accelerations4, e->device) : nullptr;
+    if (mp && mm && (!velocities4 || mv) && (!accelerations4 || ma)) {
+        EN_CK(e, nbody::host_gather(mp, mm, mv, ma, pos, vel, acc, s.n, e->stream));
+    } else {
+        EN_CK(e, cudaMemcpyAsync(e->stage, positions4, nb, cudaMemcpyHostToDevice, e->stream));
+        EN_CK(e, cudaMemcpyAsync(e->stage + s.n, masses4, nb, cudaMemcpyHostToDevice, e->stream));
+        EN_CK(e, nbody::pack_state(e->stage, e->stage + s.n, pos, s.n, e->stream));
+        if (velocities4) EN_CK(e, cudaMemcpyAsync(vel, velocities4, nb, cudaMemcpyHostToDevice, e->stream));
+        else EN_CK(e, cudaMemsetAsync(vel, 0, nb, e->stream));
+        if (accelerations4) EN_CK(e, cudaMemcpyAsync(acc, accelerations4, nb, cudaMemcpyHostToDevice, e->stream));
+        else EN_CK(e, cudaMemsetAsync(acc, 0, nb, e->stream));
+    }
     if (!pp) {
         iota_kernel<<<blocks_for(s.n, 256), 256, 0, e->stream>>>(e->bh_ids[e->bh_va] + s.first, s.n);
         EN_CK(e, cudaGetLastError());
@@ -689,6 +698,27 @@ int nbody_ensemble_download(nbody_ensemble *e, int system, float *positions4, fl
     Sys &s = e->sys[system];
     if (!s.ready) return NBODY_ERR_STATE;
     const size_t nb = static_cast<size_t>(s.n) * sizeof(float4);
+    {
+        // Page-locked host arrays are written in place by one kernel, in the
+        // caller's order (a Barnes-Hut system through the inverse of its key
+        // order, built in the staging area).
+        const int dev = e->device;
+        float4 *mp = positions4 ? nbody::host_mapped(positions4, dev) : nullptr;
+        float4 *mv = velocities4 ? nbody::host_mapped(velocities4, dev) : nullptr;
+        float4 *ma = accelerations4 ? nbody::host_mapped(accelerations4, dev) : nullptr;
+        float4 *mm = masses4 ? nbody::host_mapped(masses4, dev) : nullptr;
+        if ((!positions4 || mp) && (!velocities4 || mv) && (!accelerations4 || ma) && (!masses4 || mm)) {
+            const bool pp = s.mode == NBODY_MODE_PP;
+            if (mp || mv || ma || mm)
+                EN_CK(e, nbody::host_scatter(pp ? e->pp_pos[e->pp_cur] + s.first : e->bh_pos[0] + s.first,
+                                             pp ? e->pp_vel + s.first : e->bh_vel[e->bh_va] + s.first,
+                                             pp ? e->pp_acc + s.first : e->bh_acc[e->bh_va] + s.first,
+                                             pp ? nullptr : e->bh_ids[e->bh_va] + s.first,
+                                             reinterpret_cast<int *>(e->stage), mp, mv, ma, nullptr, mm, s.n,
+                                             e->stream, e->status));
+            return read_status(e);
+        }
+    }
     if (s.mode == NBODY_MODE_PP) {
         const float4 *pos = e->pp_pos[e->pp_cur] + s.first;
         if (positions4) {

@@ -3,7 +3,7 @@
 // coherent NVLink-C2C link): one launch in and one launch out per call instead
 // of a copy per array plus pack / unpack kernels. The bytes that cross the link
 // are the same as with cudaMemcpyAsync. Callers pass device-mapped addresses
-// only (capi.cu checks every buffer with cudaPointerGetAttributes first).
+// only, as host_mapped returns them.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -40,12 +40,13 @@ __global__ void invert_ids_kernel(const int *__restrict__ ids, int *__restrict__
 
 // Device state -> the caller's arrays, walking the caller's order d so that
 // the writes into host memory are contiguous: body d is state row inv[d] (or
-// d without inv). Positions leave with w = 0; any output may be absent.
+// d without inv). Positions leave with w = 0, masses in the reference's vec4
+// layout (m, 0, 0, 0); any output may be absent.
 __global__ void host_scatter_kernel(const float4 *__restrict__ pos_mass, const float4 *__restrict__ vel,
                                     const float4 *__restrict__ acc, const int *__restrict__ inv,
                                     float4 *__restrict__ positions4, float4 *__restrict__ vel_h,
-                                    float4 *__restrict__ acc_h, float4 *__restrict__ force_h, int64_t n,
-                                    int *status) {
+                                    float4 *__restrict__ acc_h, float4 *__restrict__ force_h,
+                                    float4 *__restrict__ masses_h, int64_t n, int *status) {
     const int64_t d = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (d >= n) return;
     const int64_t i = inv ? inv[d] : d;
@@ -53,9 +54,10 @@ __global__ void host_scatter_kernel(const float4 *__restrict__ pos_mass, const f
         record_error(status, NBODY_ERR_CAPACITY);
         return;
     }
-    if (positions4) {
+    if (positions4 || masses_h) {
         const float4 p = pos_mass[i];
-        positions4[d] = make_float4(p.x, p.y, p.z, 0.f);
+        if (positions4) positions4[d] = make_float4(p.x, p.y, p.z, 0.f);
+        if (masses_h) masses_h[d] = make_float4(p.w, 0.f, 0.f, 0.f);
     }
     if (vel_h) vel_h[d] = vel[i];
     if (acc_h || force_h) {
@@ -67,6 +69,19 @@ __global__ void host_scatter_kernel(const float4 *__restrict__ pos_mass, const f
 
 }  // namespace
 
+float4 *host_mapped(const void *p, int device) {
+    if (!p || (reinterpret_cast<uintptr_t>(p) & 15u) != 0) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || a.device != device || !a.devicePointer ||
+        (reinterpret_cast<uintptr_t>(a.devicePointer) & 15u) != 0)
+        return nullptr;
+    return static_cast<float4 *>(a.devicePointer);
+}
+
 cudaError_t host_gather(const float4 *positions4, const float4 *masses4, const float4 *vel_h, const float4 *acc_h,
                         float4 *pos_mass, float4 *vel, float4 *acc, int64_t n, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
@@ -77,8 +92,8 @@ cudaError_t host_gather(const float4 *positions4, const float4 *masses4, const f
 }
 
 cudaError_t host_scatter(const float4 *pos_mass, const float4 *vel, const float4 *acc, const int *ids, int *inv,
-                         float4 *positions4, float4 *vel_h, float4 *acc_h, float4 *force_h, int64_t n,
-                         cudaStream_t stream, int *status) {
+                         float4 *positions4, float4 *vel_h, float4 *acc_h, float4 *force_h, float4 *masses_h,
+                         int64_t n, cudaStream_t stream, int *status) {
     if (n <= 0) return cudaSuccess;
     const int threads = 256;
     const unsigned blocks = static_cast<unsigned>((n + threads - 1) / threads);
@@ -88,7 +103,7 @@ cudaError_t host_scatter(const float4 *pos_mass, const float4 *vel, const float4
         invert_ids_kernel<<<blocks, threads, 0, stream>>>(ids, inv, n, status);
     }
     host_scatter_kernel<<<blocks, threads, 0, stream>>>(pos_mass, vel, acc, ids ? inv : nullptr, positions4, vel_h,
-                                                        acc_h, force_h, n, status);
+                                                        acc_h, force_h, masses_h, n, status);
     return cudaGetLastError();
 }
 

@@ -75,10 +75,14 @@ cudaError_t unpack_masses(const float4 *pos_mass, const int *ids, float4 *masses
 // (zeros in); any output may be null; with ids (device) the state is in sorted
 // order and out[ids[i]] = in[i], through the inverse order built in `inv`
 // (n ints of device scratch).
+// host_mapped: the address on `device` of a page-locked host buffer registered
+// with that device, or nullptr for any other pointer (pageable memory, device
+// memory, another device's page-locked memory, or not 16-byte aligned).
+float4 *host_mapped(const void *p, int device);
 cudaError_t host_gather(const float4 *positions4, const float4 *masses4, const float4 *vel_h, const float4 *acc_h,
                         float4 *pos_mass, float4 *vel, float4 *acc, int64_t n, cudaStream_t stream);
 cudaError_t host_scatter(const float4 *pos_mass, const float4 *vel, const float4 *acc, const int *ids, int *inv,
-                         float4 *positions4, float4 *vel_h, float4 *acc_h, float4 *force_h, int64_t n,
-                         cudaStream_t stream, int *status);
+                         float4 *positions4, float4 *vel_h, float4 *acc_h, float4 *force_h, float4 *masses_h,
+                         int64_t n, cudaStream_t stream, int *status);
 
 }  // namespace nbody

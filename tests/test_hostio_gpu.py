@@ -5,7 +5,8 @@ in place with one kernel each (n-body_gb300/csrc/hostio.cu) instead of a
 cudaMemcpyAsync per array; pageable buffers keep the copy path. Both paths
 move the same values: every array must match bit for bit, for the direct sum
 and for Barnes-Hut (whose resident state is in sorted order and is scattered
-back through the body ids), and when only some buffers are page-locked.
+back through the body ids), and when only some buffers are page-locked; the
+ensemble calls (nbody_ensemble_upload / _download) likewise.
 """
 import ctypes
 
@@ -95,3 +96,34 @@ def test_upload_without_velocities_zeroes_them(nb, cuda):
     ref = nb.ParticleSystem(pos.copy(), np.zeros_like(vel), mass)
     nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="pp").update_particle_positions(ref)
     np.testing.assert_array_equal(res[0].positions, ref.positions)
+
+
+def test_ensemble_pinned_and_pageable_paths_agree(nb, cuda):
+    """nbody_ensemble_upload / _download take the same in-place path for
+    page-locked buffers: direct-sum and Barnes-Hut systems (the latter scattered
+    back from key order), masses included, match the copy path bit for bit."""
+    torch = cuda
+    from nbody_gb300 import initializers as I
+
+    sizes = [700, 5000, 1]
+    res = {}
+    for pinned in ("none", "all", "some"):
+        with nb.Ensemble(crossover=2048) as ens:
+            ids = []
+            for k, n in enumerate(sizes):
+                sid = ens.add(n, 0.0035, 40.0, 0.25)
+                pos, vel, mass = I.plummer(n, a=50.0, seed=70 + k) if n > 1 else I.uniform_ball(n, seed=3)
+                ens.upload(sid, _system(nb, torch, pos, vel, mass, pinned))
+                ids.append((sid, n))
+            ens.step(3)
+            outs = []
+            for sid, n in ids:
+                z = np.zeros((n, 4), np.float32)
+                o = _system(nb, torch, z[:, :3].copy(), z.copy(), np.zeros(n, np.float32), pinned)
+                ens.download(sid, o)
+                outs.append(o)
+            res[pinned] = outs
+    for a, b, c in zip(res["none"], res["all"], res["some"]):
+        for name in ("positions", "velocities", "accelerations", "masses"):
+            np.testing.assert_array_equal(getattr(a, name), getattr(b, name), err_msg=name)
+            np.testing.assert_array_equal(getattr(a, name), getattr(c, name), err_msg=name)
