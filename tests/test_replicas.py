@@ -69,3 +69,16 @@ def test_reference_arm_other_ranks_exit_quietly():
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0
     assert r.stdout.strip() == ""
+
+
+def test_committed_profiles_give_the_bench_its_traffic():
+    """bench.py reads the per-launch DRAM traffic of its roofline kernels from the
+    committed ncu summaries: each must parse to a positive byte count."""
+    import bench
+
+    for kernel in ("pp_force", "bh_traverse"):
+        t = bench.profile_traffic(kernel)
+        assert t is not None and t > 0, kernel
+    per_body = bench.profile_value("pp_batch_kernel", "traffic_bytes_per_body")
+    assert per_body is not None and per_body > 0
+    assert bench.profile_traffic("no_such_kernel") is None
