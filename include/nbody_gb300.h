@@ -104,6 +104,15 @@ float nbody_get_squared_softening(const nbody_ctx *ctx);
 int nbody_update_host(nbody_ctx *ctx, float *positions4, float *velocities4, float *accelerations4,
                       const float *masses4, float *forces4, int steps);
 
+/* 1 when the host-layout calls on `device` would read or write the buffer
+ * [p, p + bytes) in place (page-locked, mapped for that device, 16-byte
+ * aligned, and page-locked over all `bytes`), 0 when they would copy it
+ * through cudaMemcpyAsync instead; NBODY_ERR_ARG for a null pointer or a
+ * non-positive size. No counterpart in the reference (its solvers take host
+ * arrays only); it lets a caller check that its buffers get the in-place
+ * path. */
+int nbody_host_in_place(const void *p, int64_t bytes, int device);
+
 /* Resident mode: state stays in HBM between calls. nbody_upload orders its
  * reads of the host arrays on the context's stream: pageable arrays may be
  * reused when it returns, page-locked ones only after the next nbody_sync,

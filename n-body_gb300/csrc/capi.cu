@@ -333,9 +333,10 @@ int nbody_upload(nbody_ctx *ctx, const float *positions4, const float *velocitie
     const size_t b4 = static_cast<size_t>(ctx->n) * sizeof(float4);
     // Page-locked host buffers are read in place by one kernel; otherwise one
     // copy per array into the staging area, then the pack kernel.
-    const float4 *mp = nbody::host_mapped(positions4, ctx->device), *mm = nbody::host_mapped(masses4, ctx->device);
-    const float4 *mv = velocities4 ? nbody::host_mapped(velocities4, ctx->device) : nullptr;
-    const float4 *ma = accelerations4 ? nbody::host_mapped(accelerations4, ctx->device) : nullptr;
+    const float4 *mp = nbody::host_mapped(positions4, b4, ctx->device);
+    const float4 *mm = nbody::host_mapped(masses4, b4, ctx->device);
+    const float4 *mv = velocities4 ? nbody::host_mapped(velocities4, b4, ctx->device) : nullptr;
+    const float4 *ma = accelerations4 ? nbody::host_mapped(accelerations4, b4, ctx->device) : nullptr;
     if (mp && mm && (!velocities4 || mv) && (!accelerations4 || ma)) {
         NB_CK(ctx, nbody::host_gather(mp, mm, mv, ma, ctx->pos[0], ctx->vel, ctx->acc, ctx->n, ctx->stream));
     } else {
@@ -378,10 +379,10 @@ int nbody_download(nbody_ctx *ctx, float *positions4, float *velocities4, float 
         // caller's order (through the inverse of the sorted order, built in the
         // staging area, when the state is sorted).
         const int dev = ctx->device;
-        float4 *mp = positions4 ? nbody::host_mapped(positions4, dev) : nullptr;
-        float4 *mv = velocities4 ? nbody::host_mapped(velocities4, dev) : nullptr;
-        float4 *ma = accelerations4 ? nbody::host_mapped(accelerations4, dev) : nullptr;
-        float4 *mf = forces4 ? nbody::host_mapped(forces4, dev) : nullptr;
+        float4 *mp = positions4 ? nbody::host_mapped(positions4, b4, dev) : nullptr;
+        float4 *mv = velocities4 ? nbody::host_mapped(velocities4, b4, dev) : nullptr;
+        float4 *ma = accelerations4 ? nbody::host_mapped(accelerations4, b4, dev) : nullptr;
+        float4 *mf = forces4 ? nbody::host_mapped(forces4, b4, dev) : nullptr;
         if ((!positions4 || mp) && (!velocities4 || mv) && (!accelerations4 || ma) && (!forces4 || mf)) {
             const bool bh = ctx->mode == NBODY_MODE_BH;
             const int *ids = (bh && ctx->ids_valid) ? ctx->ids[ctx->bh_va] : nullptr;
@@ -443,6 +444,12 @@ int nbody_sync(nbody_ctx *ctx) {
     if (!ctx) return NBODY_ERR_ARG;
     DeviceGuard dg(ctx->device);
     return read_status(ctx);
+}
+
+int nbody_host_in_place(const void *p, int64_t bytes, int device) {
+    if (!p || bytes <= 0 || device < 0) return NBODY_ERR_ARG;
+    DeviceGuard dg(device);
+    return nbody::host_mapped(p, static_cast<size_t>(bytes), device) ? 1 : 0;
 }
 
 int nbody_update_host(nbody_ctx *ctx, float *positions4, float *velocities4, float *accelerations4,

@@ -620,9 +620,10 @@ int nbody_ensemble_upload(nbody_ensemble *e, int system, const float *positions4
     float4 *acc = pp ? e->pp_acc + s.first : e->bh_acc[e->bh_va] + s.first;
     // Page-locked host arrays are read in place by one kernel; otherwise one
     // copy per array into the staging area, then the pack kernel.
-    const float4 *mp = nbody::host_mapped(positions4, e->device), *mm = nbody::host_mapped(masses4, e->device);
-    const float4 *mv = velocities4 ? nbody::host_mapped(velocities4, e->device) : nullptr;
-    const float4 *ma = accelerations4 ? nbody::host_mapped(accelerations4, e->device) : nullptr;
+    const float4 *mp = nbody::host_mapped(positions4, nb, e->device);
+    const float4 *mm = nbody::host_mapped(masses4, nb, e->device);
+    const float4 *mv = velocities4 ? nbody::host_mapped(velocities4, nb, e->device) : nullptr;
+    const float4 *ma = accelerations4 ? nbody::host_mapped(accelerations4, nb, e->device) : nullptr;
     if (mp && mm && (!velocities4 || mv) && (!accelerations4 || ma)) {
         EN_CK(e, nbody::host_gather(mp, mm, mv, ma, pos, vel, acc, s.n, e->stream));
     } else {
@@ -703,10 +704,10 @@ int nbody_ensemble_download(nbody_ensemble *e, int system, float *positions4, fl
         // caller's order (a Barnes-Hut system through the inverse of its key
         // order, built in the staging area).
         const int dev = e->device;
-        float4 *mp = positions4 ? nbody::host_mapped(positions4, dev) : nullptr;
-        float4 *mv = velocities4 ? nbody::host_mapped(velocities4, dev) : nullptr;
-        float4 *ma = accelerations4 ? nbody::host_mapped(accelerations4, dev) : nullptr;
-        float4 *mm = masses4 ? nbody::host_mapped(masses4, dev) : nullptr;
+        float4 *mp = positions4 ? nbody::host_mapped(positions4, nb, dev) : nullptr;
+        float4 *mv = velocities4 ? nbody::host_mapped(velocities4, nb, dev) : nullptr;
+        float4 *ma = accelerations4 ? nbody::host_mapped(accelerations4, nb, dev) : nullptr;
+        float4 *mm = masses4 ? nbody::host_mapped(masses4, nb, dev) : nullptr;
         if ((!positions4 || mp) && (!velocities4 || mv) && (!accelerations4 || ma) && (!masses4 || mm)) {
             const bool pp = s.mode == NBODY_MODE_PP;
             if (mp || mv || ma || mm)

@@ -4,6 +4,8 @@
 // of a copy per array plus pack / unpack kernels. The bytes that cross the link
 // are the same as with cudaMemcpyAsync. Callers pass device-mapped addresses
 // only, as host_mapped returns them.
+#include <cuda.h>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -69,7 +71,44 @@ __global__ void host_scatter_kernel(const float4 *__restrict__ pos_mass, const f
 
 }  // namespace
 
-float4 *host_mapped(const void *p, int device) {
+namespace {
+
+// cuPointerGetAttribute from the driver, looked up through the runtime so the
+// library links no libcuda; null when the driver does not offer it.
+using PointerAttrFn = CUresult (*)(void *, CUpointer_attribute, CUdeviceptr);
+
+PointerAttrFn pointer_attr() {
+    static PointerAttrFn fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return static_cast<PointerAttrFn>(nullptr);
+        }
+        return reinterpret_cast<PointerAttrFn>(f);
+    }();
+    return fn;
+}
+
+// True when [addr, addr + bytes) lies inside the registered or allocated range
+// that the driver reports for addr.
+bool range_holds(uintptr_t addr, size_t bytes) {
+    const PointerAttrFn fn = pointer_attr();
+    if (!fn) return false;
+    CUdeviceptr start = 0;
+    size_t size = 0;
+    if (fn(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, static_cast<CUdeviceptr>(addr)) != CUDA_SUCCESS ||
+        fn(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, static_cast<CUdeviceptr>(addr)) != CUDA_SUCCESS)
+        return false;
+    const uintptr_t lo = static_cast<uintptr_t>(start);
+    return addr >= lo && bytes <= size && addr - lo <= size - bytes;
+}
+
+}  // namespace
+
+float4 *host_mapped(const void *p, size_t bytes, int device) {
     if (!p || (reinterpret_cast<uintptr_t>(p) & 15u) != 0) return nullptr;
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -78,6 +117,12 @@ float4 *host_mapped(const void *p, int device) {
     }
     if (a.type != cudaMemoryTypeHost || a.device != device || !a.devicePointer ||
         (reinterpret_cast<uintptr_t>(a.devicePointer) & 15u) != 0)
+        return nullptr;
+    // The kernels touch all `bytes` through the mapped address: a buffer that
+    // is page-locked only in part (or shorter than the call's bodies) takes
+    // the copy path, whose host-side reads the driver stages itself.
+    if (!range_holds(reinterpret_cast<uintptr_t>(p), bytes) &&
+        !range_holds(reinterpret_cast<uintptr_t>(a.devicePointer), bytes))
         return nullptr;
     return static_cast<float4 *>(a.devicePointer);
 }

@@ -76,9 +76,11 @@ cudaError_t unpack_masses(const float4 *pos_mass, const int *ids, float4 *masses
 // order and out[ids[i]] = in[i], through the inverse order built in `inv`
 // (n ints of device scratch).
 // host_mapped: the address on `device` of a page-locked host buffer registered
-// with that device, or nullptr for any other pointer (pageable memory, device
-// memory, another device's page-locked memory, or not 16-byte aligned).
-float4 *host_mapped(const void *p, int device);
+// with that device whose page-locked range holds all `bytes` from p, or
+// nullptr for any other pointer (pageable memory, device memory, another
+// device's page-locked memory, a range shorter than `bytes`, or not 16-byte
+// aligned).
+float4 *host_mapped(const void *p, size_t bytes, int device);
 cudaError_t host_gather(const float4 *positions4, const float4 *masses4, const float4 *vel_h, const float4 *acc_h,
                         float4 *pos_mass, float4 *vel, float4 *acc, int64_t n, cudaStream_t stream);
 cudaError_t host_scatter(const float4 *pos_mass, const float4 *vel, const float4 *acc, const int *ids, int *inv,

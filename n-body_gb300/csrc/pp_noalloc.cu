@@ -9,6 +9,7 @@
 // input and output buffers; the kernel's scratch (status word, per-i-block
 // arrival counters, per-slice partial accelerations) lives in one fixed-size
 // array in device memory defined in this file.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -28,16 +29,52 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 unsigned char *g_scratch_addr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};
 
-// Set-up, once per device, with that device current.
+// Driver entry points looked up through the runtime (the library links no
+// libcuda): cuCtxGetCurrent and cuCtxGetId.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+
+void *driver_fn(const char *name) {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return f;
+}
+
+// The id of the context current on this thread (unique for the life of the
+// process, so a context made anew after cudaDeviceReset has another), or 0.
+unsigned long long current_ctx_id() {
+    static const CtxGetCurrentFn get = reinterpret_cast<CtxGetCurrentFn>(driver_fn("cuCtxGetCurrent"));
+    static const CtxGetIdFn get_id = reinterpret_cast<CtxGetIdFn>(driver_fn("cuCtxGetId"));
+    CUcontext cur = nullptr;
+    unsigned long long id = 0;
+    if (!get || !get_id || get(&cur) != CUDA_SUCCESS || !cur || get_id(cur, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Set-up, once per device, with that device current: the array's device
+// address. The address is kept with the id of the context it belongs to and
+// looked up again when the current context is another one (after
+// cudaDeviceReset the module, and with it the array, is loaded anew).
 cudaError_t scratch_address(int device, unsigned char **out) {
     if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[device]) {
+    unsigned long long ctx = current_ctx_id();
+    if (!ctx || !g_scratch_addr[device] || g_scratch_ctx[device] != ctx) {
+        // The lookup binds the device's context to this thread if none was
+        // yet, so the context is read again after it.
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
+        if (!(ctx = current_ctx_id())) return cudaErrorInitializationError;
         g_scratch_addr[device] = static_cast<unsigned char *>(p);
+        g_scratch_ctx[device] = ctx;
     }
     *out = g_scratch_addr[device];
     return cudaSuccess;

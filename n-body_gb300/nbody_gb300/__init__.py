@@ -58,6 +58,7 @@ SIGNATURES = {
     "nbody_step": (_i, [_vp, _i]),
     "nbody_download": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "nbody_sync": (_i, [_vp]),
+    "nbody_host_in_place": (_i, [_vp, _i64, _i]),
     "nbody_device_state": (_i, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
     "nbody_pp_forces_device": (_i, [_vp, _vp, _vp, _i64]),
     "nbody_pp_step_device": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _i64]),

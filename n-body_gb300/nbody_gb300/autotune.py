@@ -109,14 +109,14 @@ def load_or_tune(device: int = 0, path: str | None = None, retune: bool = False,
         with open(path) as f:
             d = json.load(f)
         if d.get("version") == VERSION and d.get("device_name") == name:
-            d["source"] = path
+            d["source"] = os.path.basename(path)
             return d
     d = tune(device=device, verbose=verbose)
     try:
         os.makedirs(os.path.dirname(path), exist_ok=True)
         with open(path, "w") as f:
             json.dump(d, f, indent=1)
-        d["source"] = path
+        d["source"] = os.path.basename(path)
     except OSError:
         d["source"] = "not stored"
     return d

@@ -1,10 +1,15 @@
-"""Runs the ragged Plummer ensemble workload and prints its step time:
+"""Command-line tool for users of the ensemble API: builds the ragged
+Plummer ensemble on the device, steps it, and prints its step time and body
+counts as one JSON line, so a user can check the batched solver on their own
+GPU (and size an ensemble) without writing code:
 
     python -m nbody_gb300.run_ensemble [--systems 2048] [--steps 50] [--graph-steps 10]
 
 Systems: Plummer clusters (a = 50, m = 1, truncated at 20 a), N log-uniform in
 [256, 131072], eps^2 = 40, dt = 0.0035, theta = 0.5, direct sum below the
-tuned crossover. Also the command the ensemble kernels are profiled with.
+tuned crossover (or --crossover). It needs no host arrays: states are made by
+the device generator. The same command, at a small --systems, is the one the
+ensemble kernels are profiled with.
 """
 from __future__ import annotations
 

@@ -23,7 +23,6 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libnbody_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libnbody_ref.so")
-REFERENCE_DIR = "/root/reference"
 
 _f = ctypes.POINTER(ctypes.c_float)
 _d = ctypes.POINTER(ctypes.c_double)
@@ -34,11 +33,24 @@ _port = None
 _ref = None
 
 
+def reference_dir() -> str | None:
+    """The reference checkout: $NBODY_REFERENCE_DIR, else the Makefile's REF
+    default; None when neither holds the reference's sources (as on hosts
+    that carry only the fixtures)."""
+    d = os.environ.get("NBODY_REFERENCE_DIR")
+    if not d:
+        r = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "print-ref"], capture_output=True,
+                           text=True)
+        d = r.stdout.strip() if r.returncode == 0 else ""
+    return d if d and os.path.isdir(os.path.join(d, "src")) else None
+
+
 def build(reference: bool = True) -> None:
     """Compile the port (always) and the reference build (when its sources exist)."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
-    if reference and os.path.isdir(os.path.join(REFERENCE_DIR, "src")):
-        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", f"REF={REFERENCE_DIR}"], check=True)
+    ref_dir = reference_dir() if reference else None
+    if ref_dir:
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", f"REF={ref_dir}"], check=True)
 
 
 def _p(a, t=_f):

@@ -9,9 +9,10 @@ import subprocess
 
 import pytest
 
+import pyoracle
 from conftest import ROOT
 
-REF = "/root/reference"
+REF = pyoracle.reference_dir()
 
 PROGRAM = r"""
 #include <cstdio>
@@ -39,7 +40,7 @@ int main() {
 """
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include")), reason="reference checkout absent")
+@pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "include")), reason="reference checkout absent")
 def test_adapter_compiles_links_and_runs(nb, oracle, tmp_path):
     oracle.build(reference=True)
     objdir = os.path.join(ROOT, "oracle", "_ref", "obj")
@@ -57,4 +58,13 @@ def test_adapter_compiles_links_and_runs(nb, oracle, tmp_path):
     assert r.returncode == 0, r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stderr
-    assert out.stdout.startswith("no-device") or out.stdout.startswith("uses_gpu 0"), out.stdout
+    try:
+        import torch
+
+        gpu = torch.cuda.is_available()
+    except ImportError:
+        gpu = False
+    if gpu:
+        assert out.stdout.startswith("uses_gpu 0"), out.stdout
+    else:
+        assert out.stdout.startswith("no-device") or out.stdout.startswith("uses_gpu 0"), out.stdout

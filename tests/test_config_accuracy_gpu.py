@@ -7,9 +7,11 @@ error is the method's when the GPU's FP64 error matches the port's.
                                                    config's 100 steps, positions within 1e-4 of
                                                    the -v 2 port and no farther than the port
                                                    from an FP64 run
-  config 2, Barnes-Hut theta = 0.5, N = 2^20:     RMS <= 1.2e-3 (gate 1e-3 at theta = 0.5;
-                                                   measured 9.7e-4); after the config's 10 steps,
-                                                   forces and positions against the -v 6 port
+  config 2, Barnes-Hut theta = 0.5, N = 2^20:     RMS <= 1e-3 on 8,192 bodies (the gate at
+                                                   theta = 0.5; the port's error on the same
+                                                   sample is 9.85e-4); after the config's 10
+                                                   steps, forces and positions against the
+                                                   -v 6 port
   config 3, Barnes-Hut theta = 0.6, N = 2^24 discs: RMS 1.4e-2, the method's at this theta:
                                                    a one-off run of the port on the same
                                                    2^24 bodies gave the same FP64 error
@@ -101,14 +103,24 @@ def test_config1_hundred_steps_vs_port_and_fp64(nb, cuda, oracle):
 
 
 def test_config2_barnes_hut_1m_vs_fp64(nb, cuda, oracle):
+    """The accuracy gate at theta = 0.5 (RMS <= 1e-3 against the FP64 direct
+    sum) on 8,192 sampled bodies of the 2^20 Plummer sphere, with the -v 6
+    port's error on the same sample beside it (9.85e-4 for the port; 16,384
+    samples give the same to 0.1%)."""
     from nbody_gb300 import initializers as I
 
     n = 1 << 20
-    p, m, _, a = _one_step(nb, n, "bh", 0.25, arrays=I.plummer(n, a=100.0, seed=12345))
-    idx = np.random.default_rng(1).choice(n, 1024, replace=False)
-    rms, mx = _rel(a[idx], oracle.direct_f64(p, m, 40.0, idx=idx))
-    print(f"config 2 vs FP64 (1,024 bodies): RMS {rms:.3g}, max {mx:.3g}")
-    assert rms <= 1.2e-3, (rms, mx)
+    pos, vel, mass = I.plummer(n, a=100.0, seed=12345)
+    p, m, _, a = _one_step(nb, n, "bh", 0.25, arrays=(pos, vel, mass))
+    idx = np.random.default_rng(1).choice(n, 8192, replace=False)
+    a64 = oracle.direct_f64(p, m, 40.0, idx=idx)
+    rms, mx = _rel(a[idx], a64)
+    pf = oracle.bh_run(pos, vel, np.zeros_like(pos), mass, 0.0035, 40.0, 1, theta2=0.25, patched=True)[3]
+    rms_port, mx_port = _rel(pf[idx], a64)
+    print(f"config 2 vs FP64 (8,192 bodies): GPU RMS {rms:.4g} max {mx:.3g}; port RMS {rms_port:.4g} "
+          f"max {mx_port:.3g}")
+    assert rms <= 1e-3, (rms, mx)
+    assert abs(rms - rms_port) <= 0.01 * rms_port, (rms, rms_port)
 
 
 def test_config2_ten_steps_vs_port(nb, cuda, oracle):

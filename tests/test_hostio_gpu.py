@@ -6,9 +6,11 @@ cudaMemcpyAsync per array; pageable buffers keep the copy path. Both paths
 move the same values: every array must match bit for bit, for the direct sum
 and for Barnes-Hut (whose resident state is in sorted order and is scattered
 back through the body ids), and when only some buffers are page-locked; the
-ensemble calls (nbody_ensemble_upload / _download) likewise.
+ensemble calls (nbody_ensemble_upload / _download) likewise. A buffer that is
+page-locked over only part of its length takes the copy path.
 """
 import ctypes
+import mmap
 
 import numpy as np
 import pytest
@@ -127,3 +129,46 @@ def test_ensemble_pinned_and_pageable_paths_agree(nb, cuda):
         for name in ("positions", "velocities", "accelerations", "masses"):
             np.testing.assert_array_equal(getattr(a, name), getattr(b, name), err_msg=name)
             np.testing.assert_array_equal(getattr(a, name), getattr(c, name), err_msg=name)
+
+
+def test_partly_page_locked_buffer_takes_the_copy_path(nb, cuda):
+    """The in-place kernels touch all n float4 of a buffer through its mapped
+    address, so they are used only when the page-locked range holds all of
+    them; a buffer registered over its first half goes through
+    cudaMemcpyAsync and moves the same values."""
+    torch = cuda
+    from nbody_gb300 import initializers as I
+
+    n = 4096
+    nbytes = n * 16
+    L = nb.lib()
+    page = mmap.PAGESIZE
+    buf = mmap.mmap(-1, nbytes + page)
+    arr = np.frombuffer(buf, dtype=np.float32, count=n * 4).reshape(n, 4)
+    ptr = arr.ctypes.data
+    assert ptr % page == 0
+    assert L.nbody_host_in_place(ctypes.c_void_p(ptr), nbytes, 0) == 0  # pageable
+    half = nbytes // 2
+    cudart = torch.cuda.cudart()
+    err = cudart.cudaHostRegister(ptr, half, 0)
+    assert int(err) == 0, err
+    try:
+        assert L.nbody_host_in_place(ctypes.c_void_p(ptr), half, 0) == 1
+        assert L.nbody_host_in_place(ctypes.c_void_p(ptr), nbytes, 0) == 0
+        assert L.nbody_host_in_place(ctypes.c_void_p(ptr + half - 16), 32, 0) == 0
+        pinned = _pin(torch, np.zeros((n, 4), np.float32))
+        assert L.nbody_host_in_place(ctypes.c_void_p(pinned.ctypes.data), nbytes, 0) == 1
+        assert L.nbody_host_in_place(None, nbytes, 0) == nb.ERR_ARG
+
+        pos, vel, mass = I.plummer(n, a=50.0, seed=31)
+        ref = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+        part = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+        arr[:] = part.positions
+        part.positions = arr
+        for s in (ref, part):
+            solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="bh", theta2=0.25)
+            solver.update_particle_positions(s, steps=2)
+            solver.close()
+        _same(part, ref)
+    finally:
+        assert int(cudart.cudaHostUnregister(ptr)) == 0

@@ -24,8 +24,18 @@ def _check(got, ref):
     assert rms <= 1e-5 and mx <= 1e-3, (rms, mx)
 
 
-@pytest.mark.parametrize("n", [16384, 5000])
-def test_noalloc_matches_allocating_entry_point_twice(nb, cuda, n):
+# Sizes chosen for the plan the fixed 8 MiB array leaves (GB300, 152 SMs):
+#   16,384 / 5,000: j-slices whose partial sums fit as planned;
+#   131,072: the linear split, whose partials (5 MB) fit;
+#   262,144: the linear partials (10 MB) do not fit, the plan falls back to
+#            j-slices and cuts them to one;
+#   4,194,304: the largest size accepted, one slice;
+#   16,384 with NBODY_PP_SLICES=64: 16 MiB of slices, lowered to 31 to fit.
+CASES = [(16384, None), (5000, None), (131072, None), (262144, None), (4194304, None), (16384, "64")]
+
+
+@pytest.mark.parametrize("n,slices", CASES)
+def test_noalloc_matches_allocating_entry_point_twice(nb, cuda, monkeypatch, n, slices):
     torch = cuda
     from nbody_gb300 import initializers as I
 
@@ -40,6 +50,8 @@ def test_noalloc_matches_allocating_entry_point_twice(nb, cuda, n):
     ref_h = ref.cpu().numpy()
     solver.close()
 
+    if slices is not None:
+        monkeypatch.setenv("NBODY_PP_SLICES", slices)
     L = nb.lib()
     outs = []
     for _ in range(2):
