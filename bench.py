@@ -104,7 +104,7 @@ class ClockSampler:
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
 
     def __init__(self, device_index: int):
         self.dev = device_index
@@ -137,7 +137,7 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        sm, mx, reasons = [], [], set()
+        sm, mx, util, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
@@ -151,10 +151,18 @@ class ClockSampler:
             for name, val in zip(names, parts[5:9]):
                 if val.lower() == "active":
                     reasons.add(name)
+            if len(parts) > 9:
+                try:
+                    util.append(float(parts[9]))
+                except ValueError:
+                    pass
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+               "samples": len(sm)}
+        if util:
+            out["util_pct"] = round(statistics.fmean(util), 1)
+        return out
 
 
 def dist_env():
@@ -635,7 +643,36 @@ def bench_ensemble(args, world, rank, local, dist, steps=None):
 SERVE_BUDGET = 150e9
 
 
-def bench_serving(args, world, rank, local, dist, rates=(10.0, 100.0, 1000.0), count=None):
+BOUND_N = 1 << 20  # a single Barnes-Hut system of this size already fills the GPU (16,384 walk warps)
+
+
+def _served_checks(reqs, served, alone):
+    """Each served result against the same request run alone by the plain
+    solver: Barnes-Hut bit for bit, direct sum within FP32 summation order."""
+    bh_equal, n_bh, pp_err = 0, 0, 0.0
+    for r in reqs:
+        a, b = served.get(r.rid), alone.get(r.rid)
+        if a is None or b is None or not (a.ok and b.ok):
+            continue
+        if a.mode == "bh":
+            n_bh += 1
+            bh_equal += int(np.array_equal(a.system.positions, b.system.positions) and
+                            np.array_equal(a.system.velocities, b.system.velocities))
+        else:
+            ga, gb = a.system.accelerations[:, :3], b.system.accelerations[:, :3]
+            rel = np.linalg.norm(ga - gb, axis=1) / np.maximum(np.linalg.norm(gb, axis=1), 1e-30)
+            pp_err = max(pp_err, float(np.sqrt(np.mean(rel ** 2))))
+    return {"bh_requests_bit_equal_alone": f"{bh_equal}/{n_bh}", "pp_requests_max_accel_rms_rel_vs_alone": pp_err}
+
+
+def bench_serving(args, world, rank, local, dist, rates=(10.0, 100.0, 1000.0), count=None, pressure=True):
+    """Config 5. The same requests (sizes, steps, seeds) arrive as Poisson
+    streams at each rate. The plain solver serves them one at a time (FIFO),
+    measured once in real time on the fastest stream with the phases of every
+    service timed; its latencies at the slower rates follow from the FIFO
+    recurrence over those service times (serving.fifo_replay). The lane server
+    is measured in real time at every rate. GPU utilisation comes from
+    nvidia-smi samples restricted to each arm."""
     import torch
 
     import nbody_gb300 as nb  # noqa: F401  (loads the library)
@@ -645,62 +682,106 @@ def bench_serving(args, world, rank, local, dist, rates=(10.0, 100.0, 1000.0), c
     tune = autotune.load_or_tune(local)
     X, shape = int(tune["crossover"]), tune["pp_shape"]
     count = int(count or args.requests)
+    fast = max(rates)
+    base = serving.poisson_trace(count, rate=fast, seed=11 + rank)
+
+    # warm-up (module load, first allocations), untimed
+    serving.run_fifo_plain([serving.Request(rid=-1, n=4096, steps=3, dt=0.001, eps2=10.0)], device=local,
+                           crossover=X, realtime=False)
+    sampler = ClockSampler(local)
+    sampler.start()
+    fifo = serving.run_fifo_plain(base, device=local, crossover=X, realtime=True, timing=True)
+    fifo_clocks = sampler.stop()
+    service = {rid: r.completed - r.admitted for rid, r in fifo.items()}
+    phases = {k: round(sum(r.timing.get(k, 0.0) for r in fifo.values() if r.timing), 3)
+              for k in ("setup", "steps", "download", "teardown")}
+    stages = {}
+    for r in fifo.values():
+        for k, v in ((r.timing or {}).get("stages") or {}).items():
+            stages[k] = stages.get(k, 0.0) + v / 1e3
+    t_fifo = sum(service.values())
+    kernel_s = sum(stages.values())
+    large = [r for r in base if r.n >= BOUND_N and fifo[r.rid].ok]
+    t_large = sum(fifo[r.rid].timing["steps"] for r in large)
+    bound = t_fifo / max(1e-9, t_large)
+    fifo_info = {
+        "service_s_total": round(t_fifo, 3), "phases_s": phases,
+        "setup_teardown_s_per_request": round((phases["setup"] + phases["teardown"]) / max(1, len(fifo)), 5),
+        "kernel_s": round(kernel_s, 3), "gpu_kernel_busy_frac": round(kernel_s / max(1e-9, t_fifo), 4),
+        "walk_share_of_kernel_time": round(stages.get("bh_traverse", 0.0) / max(1e-9, kernel_s), 4),
+        "stages_s": {k: round(v, 3) for k, v in sorted(stages.items())},
+        "gpu_util_pct_nvidia_smi": fifo_clocks.get("util_pct"),
+        "large_requests": len(large), "large_steps_s": round(t_large, 3),
+        "large_work_share": round(sum(r.n * r.steps for r in large) / max(1, sum(r.n * r.steps for r in base)), 4),
+        "clocks": fifo_clocks}
     per_rate = []
     for rate in rates:
         reqs = serving.poisson_trace(count, rate=rate, seed=11 + rank)
         with serving.LaneServer(budget_bytes=SERVE_BUDGET, device=local, crossover=X, pp_shape=shape,
                                 max_chunk=10) as srv:
-            # warm-up request (module load, first allocations), untimed
             srv.run_trace([serving.Request(rid=-1, n=4096, steps=3, dt=0.001, eps2=10.0)], realtime=False)
             sampler = ClockSampler(local)
             sampler.start()
             served = srv.run_trace(reqs, realtime=True)
             clocks = sampler.stop()
             stats = srv.stats
-        plain = serving.run_fifo_plain(reqs, device=local, crossover=X, realtime=True)
-        # each served result against the same request run alone by the plain solver
-        bh_equal, pp_err = 0, 0.0
-        n_bh = 0
-        for r in reqs:
-            a, b = served[r.rid], plain[r.rid]
-            if not (a.ok and b.ok):
-                continue
-            if a.mode == "bh":
-                n_bh += 1
-                bh_equal += int(np.array_equal(a.system.positions, b.system.positions) and
-                                np.array_equal(a.system.velocities, b.system.velocities))
-            else:
-                ga, gb = a.system.accelerations[:, :3], b.system.accelerations[:, :3]
-                rel = np.linalg.norm(ga - gb, axis=1) / np.maximum(np.linalg.norm(gb, axis=1), 1e-30)
-                pp_err = max(pp_err, float(np.sqrt(np.mean(rel ** 2))))
+        plain = fifo if rate == fast else serving.fifo_replay(reqs, service)
         s_sum, p_sum = serving.summarize(served, reqs), serving.summarize(plain, reqs)
-        per_rate.append({"rate_req_per_s": rate, "served": s_sum, "plain_fifo": p_sum,
-                         "speedup_sims_per_s": round(s_sum["sims_per_s"] / max(1e-12, p_sum["sims_per_s"]), 3),
-                         "p99_ratio_plain_over_served": round(p_sum["p99_latency_s"] /
-                                                              max(1e-12, s_sum["p99_latency_s"]), 3),
-                         "max_in_flight": stats.max_in_flight, "chunks": stats.chunks,
-                         "peak_footprint_gb": round(stats.peak_footprint / 1e9, 2),
-                         "policy": "4 priority lanes (ensembles on CUDA streams of decreasing priority by N x steps)",
-                         "bh_requests_bit_equal_alone": f"{bh_equal}/{n_bh}",
-                         "pp_requests_max_accel_rms_rel_vs_alone": pp_err, "clocks": clocks})
-    head = max(per_rate, key=lambda d: d["rate_req_per_s"])
-    body_steps = sum(r.n * r.steps for r in serving.poisson_trace(count, rate=head["rate_req_per_s"], seed=11 + rank))
+        entry = {"rate_req_per_s": rate, "served": s_sum, "plain_fifo": p_sum,
+                 "plain_fifo_source": "measured" if rate == fast else "FIFO recurrence over the measured services",
+                 "speedup_sims_per_s": round(s_sum["sims_per_s"] / max(1e-12, p_sum["sims_per_s"]), 3),
+                 "p50_ratio_plain_over_served": round(p_sum["p50_latency_s"] / max(1e-12, s_sum["p50_latency_s"]), 3),
+                 "p99_ratio_plain_over_served": round(p_sum["p99_latency_s"] / max(1e-12, s_sum["p99_latency_s"]), 3),
+                 "max_in_flight": stats.max_in_flight, "chunks": stats.chunks,
+                 "peak_footprint_gb": round(stats.peak_footprint / 1e9, 2),
+                 "gpu_util_pct_nvidia_smi": clocks.get("util_pct"), "clocks": clocks}
+        entry.update(_served_checks(reqs, served, fifo))
+        per_rate.append(entry)
+        del served
+    out_pressure = None
+    if pressure:
+        # Admission under memory pressure: a budget of 1.5x the largest request's
+        # footprint, so requests queue for memory as well as for the GPU.
+        sub = base[: max(8, count // 2)]
+        with serving.LaneServer(budget_bytes=1.0, device=local, crossover=X, pp_shape=shape, max_chunk=10) as srv:
+            budget = int(1.5 * max(srv.footprint(r) for r in sub))
+            srv.budget = budget
+            t0 = time.perf_counter()
+            served = srv.run_trace(sub, realtime=True)
+            wall = time.perf_counter() - t0
+            stats = srv.stats
+        waits = [r.admitted - r.arrival for r in served.values() if r.ok]
+        out_pressure = {"requests": len(sub), "rate_req_per_s": fast, "budget_gb": round(budget / 1e9, 2),
+                        "completed": sum(r.ok for r in served.values()), "wall_s": round(wall, 3),
+                        "max_in_flight": stats.max_in_flight, "peak_footprint_gb": round(stats.peak_footprint / 1e9, 2),
+                        "admission_wait_p50_s": round(serving.percentile(waits, 50), 4),
+                        "admission_wait_p99_s": round(serving.percentile(waits, 99), 4),
+                        "summary": serving.summarize(served, sub)}
+        out_pressure.update(_served_checks(sub, served, fifo))
+        del served
+    head = per_rate[-1] if per_rate[-1]["rate_req_per_s"] == fast else max(per_rate, key=lambda d: d["rate_req_per_s"])
+    body_steps = sum(r.n * r.steps for r in base)
     return {"metric": METRIC, "component": "served sims/s", "value": head["served"]["sims_per_s"] * world,
             "unit": "sims/s", "n_gpus": world, "steps": None, "warmup": 1, "ms_per_step": None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"serving: {count} requests per rate, Poisson arrivals; Plummer a=100 or uniform "
                                    f"ball R=100, N log-uniform in [1024, 4194304], steps U[10, 500], dt in "
                                    f"{{0.001, 0.0035}}, eps2 U[10, 40], theta=0.5; admission by HBM footprint under "
-                                   f"150 GB; continuous batching in chunks of <= 10 steps, in 4 priority lanes by N x steps", "requests": count,
-                       "rates": list(rates), "crossover": X, "pp_shape": shape,
-                       "body_steps_per_trace": int(body_steps), "parallelism": "replicas"},
+                                   f"150 GB; continuous batching in chunks of <= 10 steps, in 4 priority lanes by "
+                                   f"N x steps", "requests": count, "rates": list(rates), "crossover": X,
+                       "pp_shape": shape, "body_steps_per_trace": int(body_steps), "parallelism": "replicas"},
             "p50_latency_s": head["served"]["p50_latency_s"], "p99_latency_s": head["served"]["p99_latency_s"],
             "plain_fifo": head["plain_fifo"], "speedup_vs_plain": head["speedup_sims_per_s"],
-            "per_rate": per_rate, "clocks": head["clocks"],
+            "attainable_speedup_bound": {
+                "value": round(bound, 3),
+                "how": f"FIFO service time of all requests / FIFO stepping time of the requests with N >= {BOUND_N} "
+                       f"(each already fills the GPU: its walk has >= 16,384 warps). Batching cannot make those "
+                       f"steps faster, so no schedule beats this ratio even if every smaller request were free."},
+            "fifo_plain": fifo_info, "per_rate": per_rate, "memory_pressure": out_pressure,
+            "clocks": head["clocks"],
             "e2e": {"value": head["served"]["sims_per_s"] * world, "unit": "sims/s",
                     "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": int(sum(4 * 16 * r.n for r in serving.poisson_trace(count, rate=1.0,
-                                                                                               seed=11 + rank))),
+                    "d2h_bytes_per_step": int(sum(4 * 16 * r.n for r in base)),
                     "note": "requests are generated on the device from their seeds; every result is downloaded "
                             "(4 vec4 arrays) before it counts as complete, inside the measured latency"}}
 
@@ -928,7 +1009,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", choices=["bh", "discs", "pp", "ensemble", "serving"], default="bh")
-    ap.add_argument("--requests", type=int, default=32, help="requests per rate of the serving workload")
+    ap.add_argument("--requests", type=int, default=48, help="requests per rate of the serving workload")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-pp", action="store_true", help="leave the nested direct-sum measurement out")
@@ -979,9 +1060,10 @@ def main():
                                                 "e2e", "clocks", "gpu_launches", "config", "cpu_baseline")
                              if k in dl}
         if not args.no_serving and args.workload == "bh":
-            sv = bench_serving(args, world, rank, local, dist, rates=(100.0,), count=12)
+            sv = bench_serving(args, world, rank, local, dist)
             line["serving"] = {k: sv[k] for k in ("component", "value", "unit", "p50_latency_s", "p99_latency_s",
-                                                  "plain_fifo", "speedup_vs_plain", "per_rate", "config", "e2e")
+                                                  "plain_fifo", "speedup_vs_plain", "attainable_speedup_bound",
+                                                  "fifo_plain", "per_rate", "memory_pressure", "config", "e2e")
                                if k in sv}
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -940,64 +940,22 @@ __device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, 
     }
 }
 
-// POT also accumulates the potential -sum m / sqrt(d^2 + eps^2) over the same
-// accepted records (for the energy diagnostic) into phi_out[ids[b]].
-// SEG: an ensemble of systems; warp w serves work[w] = {system, first body
-// of the warp, first body of the system, end of the system}, walks only the
-// system's records [P[first], P[end]) and takes dt, eps2, theta2 and the
-// integrator from params[system] = {dt, eps2, theta2, euler}.
-// GUARD keeps the reference's explicit d2 > 0 and leaf tests; without it
-// (eps2 > 0, no potential) they are implied: a leaf's s2 = -1 is below
-// theta2 * d2 >= 0, and a record at zero distance adds dx * w = +0 to every
-// component, so the accepted set and the sums are the same bit for bit.
-template <bool COUNT, bool POT, bool SEG, bool GUARD>
-__global__ void __launch_bounds__(256, SEG ? 5 : (POT ? 1 : 6)) traverse2_kernel(const BHNode *__restrict__ nodes,
-                                                        const uint32_t *__restrict__ node_total,
-                                                        const float4 *__restrict__ pos, int64_t n, float eps2,
-                                                        float theta2, float dt, float4 *__restrict__ pos_out,
-                                                        float4 *__restrict__ vel, float4 *__restrict__ acc,
-                                                        float4 *__restrict__ force_out, const int *__restrict__ ids,
-                                                        unsigned long long *__restrict__ counters,
-                                                        float *__restrict__ phi_out, int euler,
-                                                        const int4 *__restrict__ work, int nwork,
-                                                        const float4 *__restrict__ params,
-                                                        const uint32_t *__restrict__ P) {
-    unsigned long long n_pairs = 0, n_visits = 0;
-    float phiA = 0.f, phiB = 0.f;
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    int64_t base, end;
-    int i, m_nodes;
-    if (SEG) {
-        // Only what the walk needs stays live through it; the body range, dt
-        // and the integrator are read again afterwards.
-        if (warp >= nwork) return;  // whole warps
-        const int4 ww = work[warp];
-        const float4 prm = params[ww.x];
-        eps2 = prm.y;
-        theta2 = prm.z;
-        base = ww.y;
-        end = ww.w;
-        i = static_cast<int>(P[ww.z]);
-        m_nodes = static_cast<int>(P[ww.w]);
-    } else {
-        base = warp * 64;
-        end = n;
-        i = 0;
-        m_nodes = static_cast<int>(*node_total);
-    }
-    bool vA = base + lane < end, vB = base + lane + 32 < end;
-    const float4 meA0 = vA ? pos[base + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 meB0 = vB ? pos[base + lane + 32] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float2 nx = make_float2(-meA0.x, -meB0.x), ny = make_float2(-meA0.y, -meB0.y),
-                 nz = make_float2(-meA0.z, -meB0.z);
-    const float2 th = make_float2(theta2, theta2);
-    int skipA = vA ? i : m_nodes, skipB = vB ? i : m_nodes;
-    // Force sums of the lane's two bodies as packed pairs (x: body A, y: body B);
-    // an FFMA2 rounds each half exactly as a scalar FFMA.
-    float2 fx = make_float2(0.f, 0.f), fy = make_float2(0.f, 0.f), fz = make_float2(0.f, 0.f);
+// The union walk over the records [i, iend) (the whole tree, or the subtree
+// of record i) for the lane's bodies whose flags vA / vB are set, all active
+// at record i: each evaluates the reference criterion on the records it has
+// not covered (skip <= i); an accepted record adds its force and sets skip to
+// the record's `next`; the warp descends if any lane opened the record, else
+// jumps to the smallest skip. Sums go to fx, fy, fz (x: body A, y: body B).
+template <bool COUNT, bool POT, bool GUARD>
+__device__ __forceinline__ void union_range(const BHNode *__restrict__ nodes, const float4 *__restrict__ pos,
+                                            int64_t n, int i, const int iend, const bool vA, const bool vB,
+                                            const float2 nx, const float2 ny, const float2 nz, const float2 th,
+                                            const float eps2, float2 &fx, float2 &fy, float2 &fz, float &phiA,
+                                            float &phiB, unsigned long long &n_pairs,
+                                            unsigned long long &n_visits) {
     const float2 e2 = make_float2(eps2, eps2);
-    while (i < m_nodes) {
+    int skipA = vA ? i : iend, skipB = vB ? i : iend;
+    while (i < iend) {
         const float4 cm = __ldg(&nodes[i].cm);
         const int4 meta = __ldg(&nodes[i].meta);
         const bool actA = skipA <= i, actB = skipB <= i;
@@ -1061,6 +1019,65 @@ __global__ void __launch_bounds__(256, SEG ? 5 : (POT ? 1 : 6)) traverse2_kernel
             i = nx2 > i ? nx2 : i + 1;
         }
     }
+}
+
+// POT also accumulates the potential -sum m / sqrt(d^2 + eps^2) over the same
+// accepted records (for the energy diagnostic) into phi_out[ids[b]].
+// SEG: an ensemble of systems; warp w serves work[w] = {system, first body
+// of the warp, first body of the system, end of the system}, walks only the
+// system's records [P[first], P[end]) and takes dt, eps2, theta2 and the
+// integrator from params[system] = {dt, eps2, theta2, euler}.
+// GUARD keeps the reference's explicit d2 > 0 and leaf tests; without it
+// (eps2 > 0, no potential) they are implied: a leaf's s2 = -1 is below
+// theta2 * d2 >= 0, and a record at zero distance adds dx * w = +0 to every
+// component, so the accepted set and the sums are the same bit for bit.
+template <bool COUNT, bool POT, bool SEG, bool GUARD>
+__global__ void __launch_bounds__(256, SEG ? 5 : (POT ? 1 : 6)) traverse2_kernel(const BHNode *__restrict__ nodes,
+                                                        const uint32_t *__restrict__ node_total,
+                                                        const float4 *__restrict__ pos, int64_t n, float eps2,
+                                                        float theta2, float dt, float4 *__restrict__ pos_out,
+                                                        float4 *__restrict__ vel, float4 *__restrict__ acc,
+                                                        float4 *__restrict__ force_out, const int *__restrict__ ids,
+                                                        unsigned long long *__restrict__ counters,
+                                                        float *__restrict__ phi_out, int euler,
+                                                        const int4 *__restrict__ work, int nwork,
+                                                        const float4 *__restrict__ params,
+                                                        const uint32_t *__restrict__ P) {
+    unsigned long long n_pairs = 0, n_visits = 0;
+    float phiA = 0.f, phiB = 0.f;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    int64_t base, end;
+    int i, m_nodes;
+    if (SEG) {
+        // Only what the walk needs stays live through it; the body range, dt
+        // and the integrator are read again afterwards.
+        if (warp >= nwork) return;  // whole warps
+        const int4 ww = work[warp];
+        const float4 prm = params[ww.x];
+        eps2 = prm.y;
+        theta2 = prm.z;
+        base = ww.y;
+        end = ww.w;
+        i = static_cast<int>(P[ww.z]);
+        m_nodes = static_cast<int>(P[ww.w]);
+    } else {
+        base = warp * 64;
+        end = n;
+        i = 0;
+        m_nodes = static_cast<int>(*node_total);
+    }
+    bool vA = base + lane < end, vB = base + lane + 32 < end;
+    const float4 meA0 = vA ? pos[base + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 meB0 = vB ? pos[base + lane + 32] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 nx = make_float2(-meA0.x, -meB0.x), ny = make_float2(-meA0.y, -meB0.y),
+                 nz = make_float2(-meA0.z, -meB0.z);
+    const float2 th = make_float2(theta2, theta2);
+    // Force sums of the lane's two bodies as packed pairs (x: body A, y: body B);
+    // an FFMA2 rounds each half exactly as a scalar FFMA.
+    float2 fx = make_float2(0.f, 0.f), fy = make_float2(0.f, 0.f), fz = make_float2(0.f, 0.f);
+    union_range<COUNT, POT, GUARD>(nodes, pos, n, i, m_nodes, vA, vB, nx, ny, nz, th, eps2, fx, fy, fz, phiA, phiB,
+                                   n_pairs, n_visits);
     if (COUNT) {
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) n_pairs += __shfl_down_sync(0xffffffffu, n_pairs, off);
@@ -1093,6 +1110,277 @@ __global__ void __launch_bounds__(256, SEG ? 5 : (POT ? 1 : 6)) traverse2_kernel
     }
     // SEG reads the positions again (an L1/L2 hit) to keep registers free
     // during the walk; the single-system walk keeps them.
+    if (vA) integrate_sorted(bA, SEG ? pos[bA] : meA0, fx.x, fy.x, fz.x, dt, pos_out, vel, acc, force_out, ids, n, euler);
+    if (vB) integrate_sorted(bB, SEG ? pos[bB] : meB0, fx.y, fy.y, fz.y, dt, pos_out, vel, acc, force_out, ids, n, euler);
+}
+
+// ------------------------------------------------- group-certified walk
+// Same per-body acceptance as traverse2_kernel, with the records that every
+// body of the warp treats alike decided once for the warp. From the box of
+// the warp's 64 bodies, a record is
+//   accepted by all  when s^2 < theta^2 * d2lo, d2lo the least squared
+//                    distance to the box in the walk's own rounding (each
+//                    step is monotone, so every body's d^2 >= d2lo and its
+//                    product >= theta^2 * d2lo: the body accepts), or when it
+//                    is a lone body (every body accepts a leaf);
+//   opened by all    when it is a plain cell and s^2 >= theta^2 * d2hi, d2hi
+//                    the largest squared distance in the same rounding;
+//   ambiguous        otherwise (and for buckets and terminal cells that are
+//                    not accepted by all).
+// The tree top is classified with the lanes working on different records:
+// each lane takes a cell opened by all and walks its children. Records
+// accepted by all are collected and summed by every body in a dense loop
+// (no criterion, no per-lane bookkeeping); the subtree of an ambiguous record
+// is walked by union_range with every body active at its root, which is
+// where each body's own walk would stand. So every body accepts exactly the
+// records of its reference walk, and sums them in a fixed order.
+constexpr int kGroupWarps = 8;   // 256-thread CTAs
+constexpr int kGroupAcc = 64;    // records accepted by all, per warp, summed when full
+constexpr int kGroupOpen = 192;  // cells opened by all whose children are pending, per warp
+constexpr int kGroupAmb = 96;    // ambiguous subtree roots pending, per warp
+
+struct GroupBox {
+    float lx, ly, lz, hx, hy, hz;
+};
+
+// 0: accepted by every body of the box; 1: opened by every body (a plain
+// cell); 2: ambiguous.
+__device__ __forceinline__ int certify(const float4 cm, const int4 meta, const GroupBox &b, const float theta2) {
+    if (meta.w == 1) return 0;  // a lone body: a leaf is always accepted
+    if (meta.w >= 2) return 2;  // a bucket: its bodies are summed one by one in the walk
+    const float s2 = __int_as_float(meta.x);
+    // per axis, the least |dx| over the box (0 inside it) and the largest, both
+    // rounded as the walk rounds cm - p
+    const float gx = fmaxf(fmaxf(__fsub_rn(b.lx, cm.x), __fsub_rn(cm.x, b.hx)), 0.f);
+    const float gy = fmaxf(fmaxf(__fsub_rn(b.ly, cm.y), __fsub_rn(cm.y, b.hy)), 0.f);
+    const float gz = fmaxf(fmaxf(__fsub_rn(b.lz, cm.z), __fsub_rn(cm.z, b.hz)), 0.f);
+    const float ux = fmaxf(fabsf(__fsub_rn(cm.x, b.lx)), fabsf(__fsub_rn(b.hx, cm.x)));
+    const float uy = fmaxf(fabsf(__fsub_rn(cm.y, b.ly)), fabsf(__fsub_rn(b.hy, cm.y)));
+    const float uz = fmaxf(fabsf(__fsub_rn(cm.z, b.lz)), fabsf(__fsub_rn(b.hz, cm.z)));
+    const float lo2 = __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
+    const float hi2 = __fadd_rn(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)), __fmul_rn(uz, uz));
+    if (s2 < __fmul_rn(theta2, lo2)) return 0;
+    if (meta.w == 0 && !(s2 < __fmul_rn(theta2, hi2))) return 1;
+    return 2;
+}
+
+// Every valid body of the lane adds the records in acc[0, na): the walk's
+// force arithmetic without the criterion (all of them are accepted).
+template <bool COUNT, bool POT, bool GUARD>
+__device__ __forceinline__ void dense_sum(const float4 *acc, int na, const bool vA, const bool vB, const float2 nx,
+                                          const float2 ny, const float2 nz, const float2 e2, float2 &fx, float2 &fy,
+                                          float2 &fz, float &phiA, float &phiB, unsigned long long &n_pairs) {
+    for (int e = 0; e < na; ++e) {
+        const float4 cm = acc[e];
+        const float2 dx = __fadd2_rn(make_float2(cm.x, cm.x), nx);
+        const float2 dy = __fadd2_rn(make_float2(cm.y, cm.y), ny);
+        const float2 dz = __fadd2_rn(make_float2(cm.z, cm.z), nz);
+        const float2 d2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
+        const float2 ee = __fadd2_rn(d2, e2);
+        const float2 inv = make_float2(rsqrt_ftz(ee.x), rsqrt_ftz(ee.y));
+        const float2 inv3 = __fmul2_rn(__fmul2_rn(inv, inv), inv);
+        const float2 mw = __fmul2_rn(make_float2(cm.w, cm.w), inv3);
+        bool useA = vA, useB = vB;
+        if (GUARD) {
+            useA = useA && cm.w > 0.f && d2.x > 0.f;
+            useB = useB && cm.w > 0.f && d2.y > 0.f;
+        }
+        const float2 w = make_float2(useA ? mw.x : 0.f, useB ? mw.y : 0.f);
+        fx = __ffma2_rn(dx, w, fx);
+        fy = __ffma2_rn(dy, w, fy);
+        fz = __ffma2_rn(dz, w, fz);
+        if (COUNT) n_pairs += (useA ? 1u : 0u) + (useB ? 1u : 0u);
+        if (POT) {
+            phiA = fmaf(useA ? -cm.w : 0.f, inv.x, phiA);
+            phiB = fmaf(useB ? -cm.w : 0.f, inv.y, phiB);
+        }
+    }
+}
+
+template <bool COUNT, bool POT, bool SEG, bool GUARD>
+__global__ void __launch_bounds__(256, COUNT ? 4 : 5) group_walk_kernel(
+    const BHNode *__restrict__ nodes, const uint32_t *__restrict__ node_total, const float4 *__restrict__ pos,
+    int64_t n, float eps2, float theta2, float dt, float4 *__restrict__ pos_out, float4 *__restrict__ vel,
+    float4 *__restrict__ acc, float4 *__restrict__ force_out, const int *__restrict__ ids,
+    unsigned long long *__restrict__ counters, float *__restrict__ phi_out, int euler, const int4 *__restrict__ work,
+    int nwork, const float4 *__restrict__ params, const uint32_t *__restrict__ P) {
+    __shared__ float4 acc_mem[kGroupWarps][kGroupAcc];
+    __shared__ int2 open_mem[kGroupWarps][kGroupOpen];
+    __shared__ int2 amb_mem[kGroupWarps][kGroupAmb];
+    unsigned long long n_pairs = 0, n_visits = 0;
+    float phiA = 0.f, phiB = 0.f;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    float4 *accl = acc_mem[threadIdx.x >> 5];
+    int2 *openl = open_mem[threadIdx.x >> 5];
+    int2 *ambl = amb_mem[threadIdx.x >> 5];
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    int64_t base, end;
+    int root, rend;
+    if (SEG) {
+        if (warp >= nwork) return;  // whole warps
+        const int4 ww = work[warp];
+        const float4 prm = params[ww.x];
+        eps2 = prm.y;
+        theta2 = prm.z;
+        base = ww.y;
+        end = ww.w;
+        root = static_cast<int>(P[ww.z]);
+        rend = static_cast<int>(P[ww.w]);
+    } else {
+        base = warp * 64;
+        end = n;
+        root = 0;
+        rend = static_cast<int>(*node_total);
+    }
+    bool vA = base + lane < end, vB = base + lane + 32 < end;
+    const float4 meA0 = vA ? pos[base + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 meB0 = vB ? pos[base + lane + 32] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 nx = make_float2(-meA0.x, -meB0.x), ny = make_float2(-meA0.y, -meB0.y),
+                 nz = make_float2(-meA0.z, -meB0.z);
+    const float2 th = make_float2(theta2, theta2);
+    const float2 e2 = make_float2(eps2, eps2);
+    float2 fx = make_float2(0.f, 0.f), fy = make_float2(0.f, 0.f), fz = make_float2(0.f, 0.f);
+
+    // The box of the warp's bodies (exact: min / max on an order-preserving
+    // integer image of the floats).
+    GroupBox box;
+    {
+        const unsigned FMAX = 0xffffffffu;
+        unsigned lo[3], hi[3];
+        const float pa[3] = {meA0.x, meA0.y, meA0.z}, pb[3] = {meB0.x, meB0.y, meB0.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const unsigned oa = ord_of(pa[a]), ob = ord_of(pb[a]);
+            const unsigned mn = min(vA ? oa : FMAX, vB ? ob : FMAX), mx = max(vA ? oa : 0u, vB ? ob : 0u);
+            lo[a] = __reduce_min_sync(0xffffffffu, mn);
+            hi[a] = __reduce_max_sync(0xffffffffu, mx);
+        }
+        box.lx = float_of(lo[0]);
+        box.ly = float_of(lo[1]);
+        box.lz = float_of(lo[2]);
+        box.hx = float_of(hi[0]);
+        box.hy = float_of(hi[1]);
+        box.hz = float_of(hi[2]);
+    }
+
+    int na = 0, no = 0, nq = 0;
+    // The root, decided by every lane alike.
+    if (root < rend) {
+        const float4 cm = __ldg(&nodes[root].cm);
+        const int4 meta = __ldg(&nodes[root].meta);
+        const int cls = certify(cm, meta, box, theta2);
+        if (COUNT) ++n_visits;
+        if (cls == 0) {
+            if (lane == 0) accl[0] = cm;
+            na = 1;
+        } else if (cls == 1) {
+            if (lane == 0) openl[0] = make_int2(root, rend);
+            no = 1;
+        } else {
+            if (lane == 0) ambl[0] = make_int2(root, rend);
+            nq = 1;
+        }
+        __syncwarp();
+    }
+    // Cells opened by all, up to 32 at a time (one per lane): their children
+    // are classified in lock step, child t of every lane's cell at step t, and
+    // appended in (step, lane) order.
+    while (no > 0) {
+        const int take = no < 32 ? no : 32;
+        int ptr = 0, pend = 0;
+        if (lane < take) {
+            const int2 c = openl[no - 1 - lane];
+            ptr = c.x + 1;
+            pend = c.y;
+        }
+        __syncwarp();
+        no -= take;
+        while (__any_sync(0xffffffffu, ptr < pend)) {
+            const bool v = ptr < pend;
+            float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
+            int4 meta = make_int4(0, 0, 0, 0);
+            int cls = 3;
+            if (v) {
+                cm = __ldg(&nodes[ptr].cm);
+                meta = __ldg(&nodes[ptr].meta);
+                cls = certify(cm, meta, box, theta2);
+                if (COUNT) ++n_visits;
+            }
+            // accepted by all: sum the buffer first if they do not fit
+            const unsigned bAcc = __ballot_sync(0xffffffffu, cls == 0);
+            if (na + __popc(bAcc) > kGroupAcc) {
+                __syncwarp();
+                dense_sum<COUNT, POT, GUARD>(accl, na, vA, vB, nx, ny, nz, e2, fx, fy, fz, phiA, phiB, n_pairs);
+                __syncwarp();
+                na = 0;
+            }
+            if (cls == 0) accl[na + __popc(bAcc & below)] = cm;
+            na += __popc(bAcc);
+            // opened by all; past the stack's room they are walked as ambiguous
+            const unsigned bOpen = __ballot_sync(0xffffffffu, cls == 1);
+            const int room = kGroupOpen - no;
+            const int ro = __popc(bOpen & below);
+            const bool to_open = cls == 1 && ro < room;
+            if (to_open) openl[no + ro] = make_int2(ptr, meta.y < pend ? meta.y : pend);
+            no += min(__popc(bOpen), room);
+            const bool to_amb = cls == 2 || (cls == 1 && !to_open);
+            const unsigned bAmb = __ballot_sync(0xffffffffu, to_amb);
+            if (nq + __popc(bAmb) > kGroupAmb) {
+                // walk the pending ambiguous subtrees now to make room
+                __syncwarp();
+                for (int q = 0; q < nq; ++q) {
+                    const int2 r = ambl[q];
+                    union_range<COUNT, POT, GUARD>(nodes, pos, n, r.x, r.y, vA, vB, nx, ny, nz, th, eps2, fx, fy,
+                                                   fz, phiA, phiB, n_pairs, n_visits);
+                }
+                __syncwarp();
+                nq = 0;
+            }
+            if (to_amb) ambl[nq + __popc(bAmb & below)] = make_int2(ptr, meta.y < pend ? meta.y : pend);
+            nq += __popc(bAmb);
+            __syncwarp();
+            // next sibling; `next` lies beyond its record, so every chain ends
+            if (v) ptr = meta.y > ptr ? meta.y : pend;
+        }
+    }
+    if (na > 0) dense_sum<COUNT, POT, GUARD>(accl, na, vA, vB, nx, ny, nz, e2, fx, fy, fz, phiA, phiB, n_pairs);
+    for (int q = 0; q < nq; ++q) {
+        const int2 r = ambl[q];
+        union_range<COUNT, POT, GUARD>(nodes, pos, n, r.x, r.y, vA, vB, nx, ny, nz, th, eps2, fx, fy, fz, phiA,
+                                       phiB, n_pairs, n_visits);
+    }
+
+    if (COUNT) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) n_pairs += __shfl_down_sync(0xffffffffu, n_pairs, off);
+        if (lane == 0) {
+            atomicAdd(&counters[0], n_pairs);
+            atomicAdd(&counters[1], n_visits);
+        }
+    }
+    if (SEG) {
+        const int4 ww = work[warp];
+        const float4 prm = params[ww.x];
+        dt = prm.x;
+        euler = prm.w != 0.f ? 1 : 0;
+        base = ww.y;
+        end = ww.w;
+    }
+    const int64_t bA = base + lane, bB = bA + 32;
+    vA = bA < end;
+    vB = bB < end;
+    if (POT) {
+        if (vA) {
+            const int d = ids ? ids[bA] : static_cast<int>(bA);
+            if (d >= 0 && d < n) phi_out[d] = phiA;
+        }
+        if (vB) {
+            const int d = ids ? ids[bB] : static_cast<int>(bB);
+            if (d >= 0 && d < n) phi_out[d] = phiB;
+        }
+        return;
+    }
     if (vA) integrate_sorted(bA, SEG ? pos[bA] : meA0, fx.x, fy.x, fz.x, dt, pos_out, vel, acc, force_out, ids, n, euler);
     if (vB) integrate_sorted(bB, SEG ? pos[bB] : meB0, fx.y, fy.y, fz.y, dt, pos_out, vel, acc, force_out, ids, n, euler);
 }
@@ -1378,12 +1666,32 @@ cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaSt
     return cudaGetLastError();
 }
 
+int bh_walk_form() {
+    const char *e = std::getenv("NBODY_BH_WALK");
+    return (e && std::strcmp(e, "union") == 0) ? kWalkUnion : kWalkGroup;
+}
+
 cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,
                         float dt, float4 *pos_out, float4 *vel, float4 *acc, float4 *force_out, const int *ids,
                         int euler, cudaStream_t st, StageTimer *timer) {
     if (timer) timer->begin(kStageTraverse, st);
     // The record count P[n] stays on the device; the kernel reads it.
-    if (w.bodies_per_lane == 2) {
+    if (w.bodies_per_lane == 2 && w.walk == kWalkGroup) {
+        const int64_t warps = (n + 63) / 64;
+        const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
+        if (w.counters)
+            group_walk_kernel<true, false, false, true><<<blocks, 256, 0, st>>>(
+                w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, w.counters,
+                nullptr, euler, nullptr, 0, nullptr, nullptr);
+        else if (eps2 > 0.f && theta2 > 0.f)
+            group_walk_kernel<false, false, false, false><<<blocks, 256, 0, st>>>(
+                w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, nullptr,
+                nullptr, euler, nullptr, 0, nullptr, nullptr);
+        else
+            group_walk_kernel<false, false, false, true><<<blocks, 256, 0, st>>>(
+                w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, nullptr,
+                nullptr, euler, nullptr, 0, nullptr, nullptr);
+    } else if (w.bodies_per_lane == 2) {
         const int64_t warps = (n + 63) / 64;
         const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
         if (w.counters)
@@ -1412,9 +1720,14 @@ cudaError_t bh_potential(const float4 *pos_sorted, int64_t n, const BHWorkspace 
                          float *phi_out, const int *ids, cudaStream_t st) {
     const int64_t warps = (n + 63) / 64;
     const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
-    traverse2_kernel<false, true, false, true><<<blocks, 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, 0.f,
-                                                                 nullptr, nullptr, nullptr, nullptr, ids, nullptr,
-                                                                 phi_out, 0, nullptr, 0, nullptr, nullptr);
+    if (w.walk == kWalkGroup)
+        group_walk_kernel<false, true, false, true><<<blocks, 256, 0, st>>>(
+            w.nodes, w.P + n, pos_sorted, n, eps2, theta2, 0.f, nullptr, nullptr, nullptr, nullptr, ids, nullptr,
+            phi_out, 0, nullptr, 0, nullptr, nullptr);
+    else
+        traverse2_kernel<false, true, false, true><<<blocks, 256, 0, st>>>(
+            w.nodes, w.P + n, pos_sorted, n, eps2, theta2, 0.f, nullptr, nullptr, nullptr, nullptr, ids, nullptr,
+            phi_out, 0, nullptr, 0, nullptr, nullptr);
     return cudaGetLastError();
 }
 
@@ -1472,7 +1785,20 @@ cudaError_t bh_ensemble_step(int64_t n, BHWorkspace &w, const BHEnsembleTables &
     if (err != cudaSuccess) return err;
     if (tm) tm->begin(kStageTraverse, st);
     const unsigned blocks = static_cast<unsigned>((static_cast<int64_t>(e.nwarps) * 32 + 255) / 256);
-    if (w.counters)
+    if (w.walk == kWalkGroup) {
+        if (w.counters)
+            group_walk_kernel<true, false, true, true><<<blocks, 256, 0, st>>>(
+                w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr, nullptr, w.counters, nullptr, 0, e.warps,
+                e.nwarps, e.params, w.P);
+        else if (e.all_soft)
+            group_walk_kernel<false, false, true, false><<<blocks, 256, 0, st>>>(
+                w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr, nullptr, nullptr, nullptr, 0, e.warps,
+                e.nwarps, e.params, w.P);
+        else
+            group_walk_kernel<false, false, true, true><<<blocks, 256, 0, st>>>(
+                w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr, nullptr, nullptr, nullptr, 0, e.warps,
+                e.nwarps, e.params, w.P);
+    } else if (w.counters)
         traverse2_kernel<true, false, true, true><<<blocks, 256, 0, st>>>(w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P,
                                                                           Vo, Ao, nullptr, nullptr, w.counters,
                                                                           nullptr, 0, e.warps, e.nwarps, e.params, w.P);

@@ -49,6 +49,11 @@ struct SegView {
     const int *fdepth = nullptr;
 };
 
+// Walk forms over the same records (same accepted set per body).
+constexpr int kWalkUnion = 0;  // one record at a time for the warp's bodies, per-lane skip links
+constexpr int kWalkGroup = 1;  // records every body of the warp treats alike decided once for the
+                               // warp (summed densely), the union walk below the others
+
 struct BHWorkspace {
     int64_t n = 0;
     uint64_t *keys[2] = {nullptr, nullptr};
@@ -69,8 +74,12 @@ struct BHWorkspace {
     unsigned long long *counter_mem = nullptr;
     unsigned long long *counters = nullptr;
     int bodies_per_lane = 1;  // traversal shape: 1 or 2 bodies per lane
+    int walk = 1;             // with 2 bodies per lane: kWalkGroup or kWalkUnion
     int64_t node_count_host = 0;
 };
+
+// The walk form: kWalkGroup, or kWalkUnion when NBODY_BH_WALK=union.
+int bh_walk_form();
 
 // Bytes of device memory for a workspace of n bodies, and its layout inside
 // `base` (base == nullptr only computes the size). The bbox counter must be

@@ -179,6 +179,7 @@ int ensure_workspace(nbody_ctx *ctx, int64_t n) {
     if (const char *e = std::getenv("NBODY_BH_BODIES_PER_LANE")) {
         if (std::atoi(e) == 1) ctx->ws.bodies_per_lane = 1;
     }
+    ctx->ws.walk = nbody::bh_walk_form();
     return NBODY_OK;
 }
 

@@ -386,6 +386,7 @@ int relayout(nbody_ensemble *e) {
             EN_CK(e, cudaMemsetAsync(e->ws.bbox_counter, 0, sizeof(unsigned) * 4, e->stream));
             EN_CK(e, cudaMemsetAsync(e->ws.counter_mem, 0, sizeof(unsigned long long) * 2, e->stream));
             e->ws.bodies_per_lane = 2;
+            e->ws.walk = nbody::bh_walk_form();
             e->ws_cap = cap;
         }
     }

@@ -49,6 +49,7 @@ class Result:
     arrival: float = 0.0
     admitted: float = 0.0
     completed: float = 0.0
+    timing: dict | None = None  # run_fifo_plain(timing=True): phases of the service, seconds
 
     @property
     def latency(self) -> float:
@@ -400,8 +401,14 @@ class LaneServer:
 
 
 def run_fifo_plain(requests, device: int = 0, crossover: int = 4096, realtime: bool = True,
-                   keep_results: bool = True, clock=time.perf_counter):
-    """The single-system solver serving the requests one at a time, in arrival order."""
+                   keep_results: bool = True, clock=time.perf_counter, timing: bool = False,
+                   stream_ptr: int | None = None):
+    """The single-system solver serving the requests one at a time, in arrival
+    order. With timing=True each Result carries the phases of its service
+    (host clock, with the stream synchronised at each boundary): `setup`
+    (context creation and the initial state), `steps`, `download`, `teardown`
+    (context destruction), and `stages`, the library's per-stage device time
+    of the steps ({stage: ms}, CUDA events on the context's stream)."""
     pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
     results: dict[int, Result] = {}
     t0 = clock()
@@ -413,14 +420,28 @@ def run_fifo_plain(requests, device: int = 0, crossover: int = 4096, realtime: b
                 time.sleep(wait)
         start = now()
         mode = "pp" if req.n < crossover else "bh"
+        tm = {} if timing else None
         try:
             s = ParticleSolverCUDA(req.dt, req.eps2, req.n, mode=mode, theta2=req.theta2, device=device)
+            if stream_ptr is not None:
+                s.set_stream(stream_ptr)
             try:
                 if req.init == "state":
                     s.upload(req.state)
                 else:
                     s.init_device(req.init, seed=req.seed, params=req.params)
+                if timing:
+                    s.sync()
+                    tm["setup"] = now() - start
+                    s.profile_enable(True)
+                    t1 = now()
                 s.step(req.steps)
+                if timing:
+                    s.sync()
+                    tm["steps"] = now() - t1
+                    tm["stages"] = {k: v[0] for k, v in s.profile_read().items()}
+                    s.profile_enable(False)
+                    t1 = now()
                 out = None
                 if keep_results:
                     z = np.zeros((req.n, 4), np.float32)
@@ -428,14 +449,34 @@ def run_fifo_plain(requests, device: int = 0, crossover: int = 4096, realtime: b
                     s.download(out, masses=True)
                 else:
                     s.sync()
+                if timing:
+                    tm["download"] = now() - t1
+                    t1 = now()
             finally:
                 s.close()
+            if timing:
+                tm["teardown"] = now() - t1
             results[req.rid] = Result(req.rid, True, mode, out, arrival=req.arrival, admitted=start,
-                                      completed=now())
+                                      completed=now(), timing=tm)
         except NBodyError as e:
             results[req.rid] = Result(req.rid, False, mode, error=str(e), arrival=req.arrival, admitted=start,
-                                      completed=now())
+                                      completed=now(), timing=tm)
     return results
+
+
+def fifo_replay(requests, service_s: dict) -> dict:
+    """Completion times of a one-at-a-time FIFO server for this arrival trace,
+    given each request's service time (seconds, by rid): a request starts when
+    it has arrived and its predecessor has finished. The service of the plain
+    solver does not depend on when a request arrived, so service times measured
+    on one trace give the FIFO latencies of the same requests on another."""
+    out: dict[int, Result] = {}
+    free = 0.0
+    for req in sorted(requests, key=lambda r: (r.arrival, r.rid)):
+        start = max(free, req.arrival)
+        free = start + float(service_s[req.rid])
+        out[req.rid] = Result(req.rid, True, arrival=req.arrival, admitted=start, completed=free)
+    return out
 
 
 def poisson_trace(count: int, rate: float, seed: int = 11, n_lo: int = 1024, n_hi: int = 4_194_304,

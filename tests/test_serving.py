@@ -157,3 +157,19 @@ def test_summary_percentiles():
     assert s["p50_latency_s"] == pytest.approx(1.495, abs=1e-3)
     assert s["p99_latency_s"] == pytest.approx(1.9801, abs=1e-3)
     assert s["sims_per_s"] == pytest.approx(100 / (99 + 1.99), rel=1e-6)
+
+
+def test_fifo_replay_is_the_fifo_recurrence():
+    """fifo_replay: a request starts at max(its arrival, the previous finish);
+    service times carried over from another trace of the same requests."""
+    from nbody_gb300 import serving
+
+    reqs = [_req(serving, 0, 10, 1, arrival=0.0), _req(serving, 1, 10, 1, arrival=0.5),
+            _req(serving, 2, 10, 1, arrival=5.0), _req(serving, 3, 10, 1, arrival=5.1)]
+    service = {0: 2.0, 1: 1.0, 2: 0.5, 3: 0.25}
+    res = serving.fifo_replay(reqs, service)
+    assert [res[i].admitted for i in range(4)] == [0.0, 2.0, 5.0, 5.5]
+    assert [res[i].completed for i in range(4)] == [2.0, 3.0, 5.5, 5.75]
+    assert res[1].latency == 2.5
+    s = serving.summarize(res, reqs)
+    assert s["completed"] == 4 and s["makespan_s"] == 5.75
