@@ -514,6 +514,34 @@ __global__ void emit_leaves_kernel(const uint64_t *__restrict__ k, int64_t n, co
     }
 }
 
+// kids[8 r + j]: the record of the j-th child of cell r in pre-order (the
+// chain r + 1, next(r + 1), ... before next(r)), -1 after the last; a cell
+// has at most 8. Leaves and buckets get no entry. For the cell walk, which
+// decides a cell's children side by side.
+__global__ void kids_kernel(const BHNode *__restrict__ nodes, const uint32_t *__restrict__ total, int64_t cap,
+                            int *__restrict__ kids) {
+    const int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t m = static_cast<int64_t>(*total) < cap ? static_cast<int64_t>(*total) : cap;
+    if (r >= m) return;
+    const int4 meta = nodes[r].meta;
+    if (__int_as_float(meta.x) < 0.f) return;  // a leaf or a bucket
+    const int64_t end = meta.y < m ? meta.y : m;
+    int k[8];
+    int64_t c = r + 1;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        k[j] = -1;
+        if (c < end) {
+            k[j] = static_cast<int>(c);
+            const int64_t nx = nodes[c].meta.y;
+            c = nx > c ? nx : end;
+        }
+    }
+    int4 *out = reinterpret_cast<int4 *>(kids + 8 * r);
+    out[0] = make_int4(k[0], k[1], k[2], k[3]);
+    out[1] = make_int4(k[4], k[5], k[6], k[7]);
+}
+
 // The reference's child order (Octree::getNextNode, src/Octree/Octree.cpp:148-153):
 // index bit a is set when the body lies below the centre on axis a (x = bit 0),
 // while a Morton digit bit is set for the upper half (x = bit 2).
@@ -1114,10 +1142,8 @@ __global__ void __launch_bounds__(256, SEG ? 5 : (POT ? 1 : 6)) traverse2_kernel
     if (vB) integrate_sorted(bB, SEG ? pos[bB] : meB0, fx.y, fy.y, fz.y, dt, pos_out, vel, acc, force_out, ids, n, euler);
 }
 
-// ------------------------------------------------- group-certified walk
-// Same per-body acceptance as traverse2_kernel, with the records that every
-// body of the warp treats alike decided once for the warp. From the box of
-// the warp's 64 bodies, a record is
+// ------------------------------------------------- deciding for a set
+// From the box of a set of bodies, a record is
 //   accepted by all  when s^2 < theta^2 * d2lo, d2lo the least squared
 //                    distance to the box in the walk's own rounding (each
 //                    step is monotone, so every body's d^2 >= d2lo and its
@@ -1126,26 +1152,14 @@ __global__ void __launch_bounds__(256, SEG ? 5 : (POT ? 1 : 6)) traverse2_kernel
 //   opened by all    when it is a plain cell and s^2 >= theta^2 * d2hi, d2hi
 //                    the largest squared distance in the same rounding;
 //   ambiguous        otherwise (and for buckets and terminal cells that are
-//                    not accepted by all).
-// The tree top is classified with the lanes working on different records:
-// each lane takes a cell opened by all and walks its children. Records
-// accepted by all are collected and summed by every body in a dense loop
-// (no criterion, no per-lane bookkeeping); the subtree of an ambiguous record
-// is walked by union_range with every body active at its root, which is
-// where each body's own walk would stand. So every body accepts exactly the
-// records of its reference walk, and sums them in a fixed order.
-constexpr int kGroupWarps = 8;   // 256-thread CTAs
-constexpr int kGroupAcc = 64;    // records accepted by all, per warp, summed when full
-constexpr int kGroupOpen = 192;  // cells opened by all whose children are pending, per warp
-constexpr int kGroupAmb = 96;    // ambiguous subtree roots pending, per warp
-
-struct GroupBox {
+//                    not accepted by all), to be decided body by body.
+struct SetBox {
     float lx, ly, lz, hx, hy, hz;
 };
 
-// 0: accepted by every body of the box; 1: opened by every body (a plain
+// 0: accepted by every body in the box; 1: opened by every body (a plain
 // cell); 2: ambiguous.
-__device__ __forceinline__ int certify(const float4 cm, const int4 meta, const GroupBox &b, const float theta2) {
+__device__ __forceinline__ int certify(const float4 cm, const int4 meta, const SetBox &b, const float theta2) {
     if (meta.w == 1) return 0;  // a lone body: a leaf is always accepted
     if (meta.w >= 2) return 2;  // a bucket: its bodies are summed one by one in the walk
     const float s2 = __int_as_float(meta.x);
@@ -1164,56 +1178,90 @@ __device__ __forceinline__ int certify(const float4 cm, const int4 meta, const G
     return 2;
 }
 
-// Every valid body of the lane adds the records in acc[0, na): the walk's
-// force arithmetic without the criterion (all of them are accepted).
+// ------------------------------------------------------------ cell walk
+// Same per-body acceptance as traverse2_kernel, organised by cells. A warp
+// holds a stack of cells that some of its bodies opened, each with the masks
+// of those bodies (first and second body of each lane) and their box. For a
+// cell popped, eight lanes load its children and decide each one for the
+// whole set from the box (certify: accepted by all of them, opened by all of
+// them, or ambiguous). Accepted children are summed by those bodies with no
+// criterion; children opened by all are pushed with the same set and box;
+// each ambiguous child gets the per-body criterion, its accepting bodies sum
+// it (or a bucket's bodies), the bodies that open a terminal cell sum its
+// bodies, and the bodies that open a plain cell are pushed with it as a new,
+// smaller set with its own box. A body thus meets exactly the records of its
+// own reference walk, and decides by itself only those its set disagrees on.
+constexpr int kCellWarps = 8;   // 256-thread CTAs
+constexpr int kCellDepth = 48;  // stack entries per warp; a full stack sends a cell to union_range
+
+// Box of the bodies in masks sa / sb (exact min / max on the order-preserving
+// integer image).
+__device__ __forceinline__ SetBox box_of(unsigned sa, unsigned sb, int lane, float4 pa, float4 pb) {
+    const bool ia = (sa >> lane) & 1u, ib = (sb >> lane) & 1u;
+    const float xa[3] = {pa.x, pa.y, pa.z}, xb[3] = {pb.x, pb.y, pb.z};
+    unsigned lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const unsigned oa = ord_of(xa[a]), ob = ord_of(xb[a]);
+        lo[a] = __reduce_min_sync(0xffffffffu, min(ia ? oa : 0xffffffffu, ib ? ob : 0xffffffffu));
+        hi[a] = __reduce_max_sync(0xffffffffu, max(ia ? oa : 0u, ib ? ob : 0u));
+    }
+    SetBox b;
+    b.lx = float_of(lo[0]);
+    b.ly = float_of(lo[1]);
+    b.lz = float_of(lo[2]);
+    b.hx = float_of(hi[0]);
+    b.hy = float_of(hi[1]);
+    b.hz = float_of(hi[2]);
+    return b;
+}
+
+// The record's force on each of the lane's bodies whose flag is set (the
+// walk's arithmetic; GUARD keeps the explicit zero-distance and massless
+// tests).
 template <bool COUNT, bool POT, bool GUARD>
-__device__ __forceinline__ void dense_sum(const float4 *acc, int na, const bool vA, const bool vB, const float2 nx,
-                                          const float2 ny, const float2 nz, const float2 e2, float2 &fx, float2 &fy,
-                                          float2 &fz, float &phiA, float &phiB, unsigned long long &n_pairs) {
-    for (int e = 0; e < na; ++e) {
-        const float4 cm = acc[e];
-        const float2 dx = __fadd2_rn(make_float2(cm.x, cm.x), nx);
-        const float2 dy = __fadd2_rn(make_float2(cm.y, cm.y), ny);
-        const float2 dz = __fadd2_rn(make_float2(cm.z, cm.z), nz);
-        const float2 d2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
-        const float2 ee = __fadd2_rn(d2, e2);
-        const float2 inv = make_float2(rsqrt_ftz(ee.x), rsqrt_ftz(ee.y));
-        const float2 inv3 = __fmul2_rn(__fmul2_rn(inv, inv), inv);
-        const float2 mw = __fmul2_rn(make_float2(cm.w, cm.w), inv3);
-        bool useA = vA, useB = vB;
-        if (GUARD) {
-            useA = useA && cm.w > 0.f && d2.x > 0.f;
-            useB = useB && cm.w > 0.f && d2.y > 0.f;
-        }
-        const float2 w = make_float2(useA ? mw.x : 0.f, useB ? mw.y : 0.f);
-        fx = __ffma2_rn(dx, w, fx);
-        fy = __ffma2_rn(dy, w, fy);
-        fz = __ffma2_rn(dz, w, fz);
-        if (COUNT) n_pairs += (useA ? 1u : 0u) + (useB ? 1u : 0u);
-        if (POT) {
-            phiA = fmaf(useA ? -cm.w : 0.f, inv.x, phiA);
-            phiB = fmaf(useB ? -cm.w : 0.f, inv.y, phiB);
-        }
+__device__ __forceinline__ void add_record(const float4 cm, bool useA, bool useB, const float2 nx, const float2 ny,
+                                           const float2 nz, const float2 e2, float2 &fx, float2 &fy, float2 &fz,
+                                           float &phiA, float &phiB, unsigned long long &n_pairs) {
+    const float2 dx = __fadd2_rn(make_float2(cm.x, cm.x), nx);
+    const float2 dy = __fadd2_rn(make_float2(cm.y, cm.y), ny);
+    const float2 dz = __fadd2_rn(make_float2(cm.z, cm.z), nz);
+    const float2 d2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
+    if (GUARD) {
+        useA = useA && cm.w > 0.f && d2.x > 0.f;
+        useB = useB && cm.w > 0.f && d2.y > 0.f;
+    }
+    const float2 ee = __fadd2_rn(d2, e2);
+    const float2 inv = make_float2(rsqrt_ftz(ee.x), rsqrt_ftz(ee.y));
+    const float2 inv3 = __fmul2_rn(__fmul2_rn(inv, inv), inv);
+    const float2 mw = __fmul2_rn(make_float2(cm.w, cm.w), inv3);
+    const float2 w = make_float2(useA ? mw.x : 0.f, useB ? mw.y : 0.f);
+    fx = __ffma2_rn(dx, w, fx);
+    fy = __ffma2_rn(dy, w, fy);
+    fz = __ffma2_rn(dz, w, fz);
+    if (COUNT) n_pairs += (useA ? 1u : 0u) + (useB ? 1u : 0u);
+    if (POT) {
+        phiA = fmaf(useA ? -cm.w : 0.f, inv.x, phiA);
+        phiB = fmaf(useB ? -cm.w : 0.f, inv.y, phiB);
     }
 }
 
 template <bool COUNT, bool POT, bool SEG, bool GUARD>
-__global__ void __launch_bounds__(256, COUNT ? 4 : 5) group_walk_kernel(
-    const BHNode *__restrict__ nodes, const uint32_t *__restrict__ node_total, const float4 *__restrict__ pos,
-    int64_t n, float eps2, float theta2, float dt, float4 *__restrict__ pos_out, float4 *__restrict__ vel,
-    float4 *__restrict__ acc, float4 *__restrict__ force_out, const int *__restrict__ ids,
+__global__ void __launch_bounds__(256, COUNT ? 4 : 5) cell_walk_kernel(
+    const BHNode *__restrict__ nodes, const int *__restrict__ kids, const uint32_t *__restrict__ node_total,
+    const float4 *__restrict__ pos, int64_t n, float eps2, float theta2, float dt, float4 *__restrict__ pos_out,
+    float4 *__restrict__ vel, float4 *__restrict__ acc, float4 *__restrict__ force_out, const int *__restrict__ ids,
     unsigned long long *__restrict__ counters, float *__restrict__ phi_out, int euler, const int4 *__restrict__ work,
     int nwork, const float4 *__restrict__ params, const uint32_t *__restrict__ P) {
-    __shared__ float4 acc_mem[kGroupWarps][kGroupAcc];
-    __shared__ int2 open_mem[kGroupWarps][kGroupOpen];
-    __shared__ int2 amb_mem[kGroupWarps][kGroupAmb];
+    __shared__ int4 stk_i[kCellWarps][kCellDepth];     // cell, mask A, mask B, -
+    __shared__ float4 stk_lo[kCellWarps][kCellDepth];  // box: lx, ly, lz, hx
+    __shared__ float2 stk_hi[kCellWarps][kCellDepth];  // box: hy, hz
     unsigned long long n_pairs = 0, n_visits = 0;
     float phiA = 0.f, phiB = 0.f;
     const int lane = threadIdx.x & 31;
-    const unsigned below = (1u << lane) - 1u;
-    float4 *accl = acc_mem[threadIdx.x >> 5];
-    int2 *openl = open_mem[threadIdx.x >> 5];
-    int2 *ambl = amb_mem[threadIdx.x >> 5];
+    int4 *si = stk_i[threadIdx.x >> 5];
+    float4 *slo = stk_lo[threadIdx.x >> 5];
+    float2 *shi = stk_hi[threadIdx.x >> 5];
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     int64_t base, end;
     int root, rend;
@@ -1241,114 +1289,131 @@ __global__ void __launch_bounds__(256, COUNT ? 4 : 5) group_walk_kernel(
     const float2 th = make_float2(theta2, theta2);
     const float2 e2 = make_float2(eps2, eps2);
     float2 fx = make_float2(0.f, 0.f), fy = make_float2(0.f, 0.f), fz = make_float2(0.f, 0.f);
+    int sp = 0;
 
-    // The box of the warp's bodies (exact: min / max on an order-preserving
-    // integer image of the floats).
-    GroupBox box;
-    {
-        const unsigned FMAX = 0xffffffffu;
-        unsigned lo[3], hi[3];
-        const float pa[3] = {meA0.x, meA0.y, meA0.z}, pb[3] = {meB0.x, meB0.y, meB0.z};
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const unsigned oa = ord_of(pa[a]), ob = ord_of(pb[a]);
-            const unsigned mn = min(vA ? oa : FMAX, vB ? ob : FMAX), mx = max(vA ? oa : 0u, vB ? ob : 0u);
-            lo[a] = __reduce_min_sync(0xffffffffu, mn);
-            hi[a] = __reduce_max_sync(0xffffffffu, mx);
-        }
-        box.lx = float_of(lo[0]);
-        box.ly = float_of(lo[1]);
-        box.lz = float_of(lo[2]);
-        box.hx = float_of(hi[0]);
-        box.hy = float_of(hi[1]);
-        box.hz = float_of(hi[2]);
-    }
-
-    int na = 0, no = 0, nq = 0;
-    // The root, decided by every lane alike.
-    if (root < rend) {
-        const float4 cm = __ldg(&nodes[root].cm);
-        const int4 meta = __ldg(&nodes[root].meta);
-        const int cls = certify(cm, meta, box, theta2);
-        if (COUNT) ++n_visits;
-        if (cls == 0) {
-            if (lane == 0) accl[0] = cm;
-            na = 1;
-        } else if (cls == 1) {
-            if (lane == 0) openl[0] = make_int2(root, rend);
-            no = 1;
+    // Record k decided body by body for the bodies in (sa, sb); the bodies
+    // that open a plain cell are pushed with it (or, on a full stack, walk
+    // its subtree with union_range).
+    auto decide = [&](int k, unsigned sa, unsigned sb) {
+        const float4 cm = __ldg(&nodes[k].cm);
+        const int4 meta = __ldg(&nodes[k].meta);
+        const bool actA = (sa >> lane) & 1u, actB = (sb >> lane) & 1u;
+        const float2 dx = __fadd2_rn(make_float2(cm.x, cm.x), nx);
+        const float2 dy = __fadd2_rn(make_float2(cm.y, cm.y), ny);
+        const float2 dz = __fadd2_rn(make_float2(cm.z, cm.z), nz);
+        const float2 d2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
+        const float s2 = __int_as_float(meta.x);
+        const float2 rhs = __fmul2_rn(th, d2);
+        bool accA, accB, useA, useB;
+        if (GUARD) {
+            accA = actA && (s2 < 0.f || s2 < rhs.x);
+            accB = actB && (s2 < 0.f || s2 < rhs.y);
+            const bool self = meta.w <= 1 && cm.w > 0.f;
+            useA = accA && self && d2.x > 0.f;
+            useB = accB && self && d2.y > 0.f;
         } else {
-            if (lane == 0) ambl[0] = make_int2(root, rend);
-            nq = 1;
+            accA = actA && s2 < rhs.x;
+            accB = actB && s2 < rhs.y;
+            const bool self = meta.w <= 1;
+            useA = accA && self;
+            useB = accB && self;
         }
-        __syncwarp();
-    }
-    // Cells opened by all, up to 32 at a time (one per lane): their children
-    // are classified in lock step, child t of every lane's cell at step t, and
-    // appended in (step, lane) order.
-    while (no > 0) {
-        const int take = no < 32 ? no : 32;
-        int ptr = 0, pend = 0;
-        if (lane < take) {
-            const int2 c = openl[no - 1 - lane];
-            ptr = c.x + 1;
-            pend = c.y;
+        if (COUNT) ++n_visits;
+        {
+            const float2 ee = __fadd2_rn(d2, e2);
+            const float2 inv = make_float2(rsqrt_ftz(ee.x), rsqrt_ftz(ee.y));
+            const float2 inv3 = __fmul2_rn(__fmul2_rn(inv, inv), inv);
+            const float2 mw = __fmul2_rn(make_float2(cm.w, cm.w), inv3);
+            const float2 w = make_float2(useA ? mw.x : 0.f, useB ? mw.y : 0.f);
+            fx = __ffma2_rn(dx, w, fx);
+            fy = __ffma2_rn(dy, w, fy);
+            fz = __ffma2_rn(dz, w, fz);
+            if (COUNT) n_pairs += (useA ? 1u : 0u) + (useB ? 1u : 0u);
+            if (POT) {
+                phiA = fmaf(useA ? -cm.w : 0.f, inv.x, phiA);
+                phiB = fmaf(useB ? -cm.w : 0.f, inv.y, phiB);
+            }
         }
-        __syncwarp();
-        no -= take;
-        while (__any_sync(0xffffffffu, ptr < pend)) {
-            const bool v = ptr < pend;
-            float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
-            int4 meta = make_int4(0, 0, 0, 0);
-            int cls = 3;
-            if (v) {
-                cm = __ldg(&nodes[ptr].cm);
-                meta = __ldg(&nodes[ptr].meta);
-                cls = certify(cm, meta, box, theta2);
-                if (COUNT) ++n_visits;
+        if (meta.w != 0 && meta.w != 1) {  // a bucket accepted, or a terminal cell opened: body by body
+            const int cntb = meta.w >= 2 ? meta.w : -meta.w;
+            const bool doA = (meta.w >= 2 && accA) || (meta.w < 0 && actA && !accA);
+            const bool doB = (meta.w >= 2 && accB) || (meta.w < 0 && actB && !accB);
+            if (COUNT || POT) {
+                const float4 meA = make_float4(-nx.x, -ny.x, -nz.x, 0.f), meB = make_float4(-nx.y, -ny.y, -nz.y, 0.f);
+                if (doA) direct_sum_range(pos, n, meta.z, cntb, meA, eps2, fx.x, fy.x, fz.x, n_pairs, COUNT, phiA, POT);
+                if (doB) direct_sum_range(pos, n, meta.z, cntb, meB, eps2, fx.y, fy.y, fz.y, n_pairs, COUNT, phiB, POT);
+            } else if (doA || doB) {
+                direct_sum_range2(pos, n, meta.z, cntb, nx, ny, nz, eps2, doA, doB, fx, fy, fz);
             }
-            // accepted by all: sum the buffer first if they do not fit
-            const unsigned bAcc = __ballot_sync(0xffffffffu, cls == 0);
-            if (na + __popc(bAcc) > kGroupAcc) {
-                __syncwarp();
-                dense_sum<COUNT, POT, GUARD>(accl, na, vA, vB, nx, ny, nz, e2, fx, fy, fz, phiA, phiB, n_pairs);
-                __syncwarp();
-                na = 0;
+            return;
+        }
+        if (meta.w != 0) return;
+        const unsigned oa = __ballot_sync(0xffffffffu, actA && !accA);
+        const unsigned ob = __ballot_sync(0xffffffffu, actB && !accB);
+        if (!(oa | ob)) return;
+        if (sp < kCellDepth) {
+            const SetBox b = box_of(oa, ob, lane, meA0, meB0);
+            if (lane == 0) {
+                si[sp] = make_int4(k, static_cast<int>(oa), static_cast<int>(ob), 0);
+                slo[sp] = make_float4(b.lx, b.ly, b.lz, b.hx);
+                shi[sp] = make_float2(b.hy, b.hz);
             }
-            if (cls == 0) accl[na + __popc(bAcc & below)] = cm;
-            na += __popc(bAcc);
-            // opened by all; past the stack's room they are walked as ambiguous
-            const unsigned bOpen = __ballot_sync(0xffffffffu, cls == 1);
-            const int room = kGroupOpen - no;
-            const int ro = __popc(bOpen & below);
-            const bool to_open = cls == 1 && ro < room;
-            if (to_open) openl[no + ro] = make_int2(ptr, meta.y < pend ? meta.y : pend);
-            no += min(__popc(bOpen), room);
-            const bool to_amb = cls == 2 || (cls == 1 && !to_open);
-            const unsigned bAmb = __ballot_sync(0xffffffffu, to_amb);
-            if (nq + __popc(bAmb) > kGroupAmb) {
-                // walk the pending ambiguous subtrees now to make room
-                __syncwarp();
-                for (int q = 0; q < nq; ++q) {
-                    const int2 r = ambl[q];
-                    union_range<COUNT, POT, GUARD>(nodes, pos, n, r.x, r.y, vA, vB, nx, ny, nz, th, eps2, fx, fy,
-                                                   fz, phiA, phiB, n_pairs, n_visits);
+            ++sp;
+        } else {
+            union_range<COUNT, POT, GUARD>(nodes, pos, n, k + 1, meta.y, (oa >> lane) & 1u, (ob >> lane) & 1u, nx,
+                                           ny, nz, th, eps2, fx, fy, fz, phiA, phiB, n_pairs, n_visits);
+        }
+    };
+
+    if (root < rend) decide(root, __ballot_sync(0xffffffffu, vA), __ballot_sync(0xffffffffu, vB));
+    while (sp > 0) {
+        --sp;
+        __syncwarp();  // lane 0's writes of the entry before every lane reads it
+        const int4 t = si[sp];
+        const float4 bl = slo[sp];
+        const float2 bh = shi[sp];
+        __syncwarp();  // every lane has read the entry before the slot is written again
+        const int c = t.x;
+        const unsigned sa = static_cast<unsigned>(t.y), sb = static_cast<unsigned>(t.z);
+        SetBox box;
+        box.lx = bl.x;
+        box.ly = bl.y;
+        box.lz = bl.z;
+        box.hx = bl.w;
+        box.hy = bh.x;
+        box.hz = bh.y;
+        // eight lanes take the cell's children and decide them for the whole set
+        int kid = -1, cls = 3;
+        if (lane < 8) {
+            kid = __ldg(&kids[8 * static_cast<int64_t>(c) + lane]);
+            if (kid >= 0) cls = certify(__ldg(&nodes[kid].cm), __ldg(&nodes[kid].meta), box, theta2);
+        }
+        const unsigned bAcc = __ballot_sync(0xffffffffu, cls == 0);
+        const unsigned bOpen = __ballot_sync(0xffffffffu, cls == 1);
+        const unsigned bAmb = __ballot_sync(0xffffffffu, cls == 2);
+        if (COUNT) n_visits += __popc(bAcc | bOpen | bAmb);
+        const bool actA = (sa >> lane) & 1u, actB = (sb >> lane) & 1u;
+        for (unsigned m = bAcc; m; m &= m - 1) {
+            const int k = __shfl_sync(0xffffffffu, kid, __ffs(m) - 1);
+            add_record<COUNT, POT, GUARD>(__ldg(&nodes[k].cm), actA, actB, nx, ny, nz, e2, fx, fy, fz, phiA, phiB,
+                                          n_pairs);
+        }
+        for (unsigned m = bOpen; m; m &= m - 1) {
+            const int k = __shfl_sync(0xffffffffu, kid, __ffs(m) - 1);
+            if (sp < kCellDepth) {
+                if (lane == 0) {
+                    si[sp] = make_int4(k, static_cast<int>(sa), static_cast<int>(sb), 0);
+                    slo[sp] = bl;
+                    shi[sp] = bh;
                 }
-                __syncwarp();
-                nq = 0;
+                ++sp;
+            } else {
+                const int kend = __ldg(&nodes[k].meta).y;
+                union_range<COUNT, POT, GUARD>(nodes, pos, n, k + 1, kend, actA, actB, nx, ny, nz, th, eps2, fx,
+                                               fy, fz, phiA, phiB, n_pairs, n_visits);
             }
-            if (to_amb) ambl[nq + __popc(bAmb & below)] = make_int2(ptr, meta.y < pend ? meta.y : pend);
-            nq += __popc(bAmb);
-            __syncwarp();
-            // next sibling; `next` lies beyond its record, so every chain ends
-            if (v) ptr = meta.y > ptr ? meta.y : pend;
         }
-    }
-    if (na > 0) dense_sum<COUNT, POT, GUARD>(accl, na, vA, vB, nx, ny, nz, e2, fx, fy, fz, phiA, phiB, n_pairs);
-    for (int q = 0; q < nq; ++q) {
-        const int2 r = ambl[q];
-        union_range<COUNT, POT, GUARD>(nodes, pos, n, r.x, r.y, vA, vB, nx, ny, nz, th, eps2, fx, fy, fz, phiA,
-                                       phiB, n_pairs, n_visits);
+        for (unsigned m = bAmb; m; m &= m - 1) decide(__shfl_sync(0xffffffffu, kid, __ffs(m) - 1), sa, sb);
     }
 
     if (COUNT) {
@@ -1553,6 +1618,7 @@ size_t bh_workspace_layout(int64_t n, void *base, BHWorkspace *w) {
     w->P = static_cast<uint32_t *>(take(sizeof(uint32_t) * (nn + 1)));
     w->scan_sums = static_cast<uint32_t *>(take(sizeof(uint32_t) * static_cast<size_t>(tiles + 1)));
     w->nodes = static_cast<BHNode *>(take(sizeof(BHNode) * 2 * nn));
+    w->kids = static_cast<int *>(take(sizeof(int) * 8 * 2 * nn));
     w->counter_mem = static_cast<unsigned long long *>(take(sizeof(unsigned long long) * 2));
     w->counters = nullptr;
     w->node_count_host = 0;
@@ -1644,6 +1710,10 @@ cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaSt
                                                                 sv, !levels);
     emit_leaves_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, pos_sorted, w.tree, w.mask, w.P, w.nodes, w.rec, sv,
                                                          !levels);
+    if (w.walk == kWalkCell) {
+        const int64_t cap = 2 * (n > 1 ? n : 2);
+        kids_kernel<<<grid_for(cap, 256), 256, 0, st>>>(w.nodes, w.P + n, cap, w.kids);
+    }
     if (timer) timer->end(kStageBuild, st);
     if (timer) timer->begin(kStageUpsweep, st);
     if (!levels) {
@@ -1666,9 +1736,28 @@ cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaSt
     return cudaGetLastError();
 }
 
+// One launch of the walk in the workspace's form (the same accepted records
+// per body in both forms).
+template <bool COUNT, bool POT, bool SEG, bool GUARD>
+void launch_walk(const BHWorkspace &w, unsigned blocks, cudaStream_t st, const uint32_t *node_total,
+                 const float4 *pos, int64_t n, float eps2, float theta2, float dt, float4 *pos_out, float4 *vel,
+                 float4 *acc, float4 *force_out, const int *ids, unsigned long long *counters, float *phi_out,
+                 int euler, const int4 *work, int nwork, const float4 *params, const uint32_t *P) {
+    if (w.walk == kWalkCell)
+        cell_walk_kernel<COUNT, POT, SEG, GUARD><<<blocks, 256, 0, st>>>(w.nodes, w.kids, node_total, pos, n, eps2,
+                                                                         theta2, dt, pos_out, vel, acc, force_out,
+                                                                         ids, counters, phi_out, euler, work, nwork,
+                                                                         params, P);
+    else
+        traverse2_kernel<COUNT, POT, SEG, GUARD><<<blocks, 256, 0, st>>>(w.nodes, node_total, pos, n, eps2, theta2,
+                                                                         dt, pos_out, vel, acc, force_out, ids,
+                                                                         counters, phi_out, euler, work, nwork,
+                                                                         params, P);
+}
+
 int bh_walk_form() {
     const char *e = std::getenv("NBODY_BH_WALK");
-    return (e && std::strcmp(e, "union") == 0) ? kWalkUnion : kWalkGroup;
+    return (e && std::strcmp(e, "union") == 0) ? kWalkUnion : kWalkCell;
 }
 
 cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,
@@ -1676,36 +1765,21 @@ cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &
                         int euler, cudaStream_t st, StageTimer *timer) {
     if (timer) timer->begin(kStageTraverse, st);
     // The record count P[n] stays on the device; the kernel reads it.
-    if (w.bodies_per_lane == 2 && w.walk == kWalkGroup) {
+    if (w.bodies_per_lane == 2) {
         const int64_t warps = (n + 63) / 64;
         const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
         if (w.counters)
-            group_walk_kernel<true, false, false, true><<<blocks, 256, 0, st>>>(
-                w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, w.counters,
-                nullptr, euler, nullptr, 0, nullptr, nullptr);
+            launch_walk<true, false, false, true>(w, blocks, st, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel,
+                                                 acc, force_out, ids, w.counters, nullptr, euler, nullptr, 0, nullptr,
+                                                 nullptr);
         else if (eps2 > 0.f && theta2 > 0.f)
-            group_walk_kernel<false, false, false, false><<<blocks, 256, 0, st>>>(
-                w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, nullptr,
-                nullptr, euler, nullptr, 0, nullptr, nullptr);
+            launch_walk<false, false, false, false>(w, blocks, st, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out,
+                                                   vel, acc, force_out, ids, nullptr, nullptr, euler, nullptr, 0,
+                                                   nullptr, nullptr);
         else
-            group_walk_kernel<false, false, false, true><<<blocks, 256, 0, st>>>(
-                w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, nullptr,
-                nullptr, euler, nullptr, 0, nullptr, nullptr);
-    } else if (w.bodies_per_lane == 2) {
-        const int64_t warps = (n + 63) / 64;
-        const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
-        if (w.counters)
-            traverse2_kernel<true, false, false, true><<<blocks, 256, 0, st>>>(
-                w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, w.counters,
-                nullptr, euler, nullptr, 0, nullptr, nullptr);
-        else if (eps2 > 0.f && theta2 > 0.f)
-            traverse2_kernel<false, false, false, false><<<blocks, 256, 0, st>>>(
-                w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, nullptr,
-                nullptr, euler, nullptr, 0, nullptr, nullptr);
-        else
-            traverse2_kernel<false, false, false, true><<<blocks, 256, 0, st>>>(
-                w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, nullptr,
-                nullptr, euler, nullptr, 0, nullptr, nullptr);
+            launch_walk<false, false, false, true>(w, blocks, st, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out,
+                                                  vel, acc, force_out, ids, nullptr, nullptr, euler, nullptr, 0,
+                                                  nullptr, nullptr);
     } else if (w.counters)
         traverse_kernel<true><<<grid_for(n, 256), 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
                                                                 pos_out, vel, acc, force_out, ids, w.counters, euler);
@@ -1720,14 +1794,8 @@ cudaError_t bh_potential(const float4 *pos_sorted, int64_t n, const BHWorkspace 
                          float *phi_out, const int *ids, cudaStream_t st) {
     const int64_t warps = (n + 63) / 64;
     const unsigned blocks = static_cast<unsigned>((warps * 32 + 255) / 256);
-    if (w.walk == kWalkGroup)
-        group_walk_kernel<false, true, false, true><<<blocks, 256, 0, st>>>(
-            w.nodes, w.P + n, pos_sorted, n, eps2, theta2, 0.f, nullptr, nullptr, nullptr, nullptr, ids, nullptr,
-            phi_out, 0, nullptr, 0, nullptr, nullptr);
-    else
-        traverse2_kernel<false, true, false, true><<<blocks, 256, 0, st>>>(
-            w.nodes, w.P + n, pos_sorted, n, eps2, theta2, 0.f, nullptr, nullptr, nullptr, nullptr, ids, nullptr,
-            phi_out, 0, nullptr, 0, nullptr, nullptr);
+    launch_walk<false, true, false, true>(w, blocks, st, w.P + n, pos_sorted, n, eps2, theta2, 0.f, nullptr, nullptr,
+                                          nullptr, nullptr, ids, nullptr, phi_out, 0, nullptr, 0, nullptr, nullptr);
     return cudaGetLastError();
 }
 
@@ -1785,31 +1853,15 @@ cudaError_t bh_ensemble_step(int64_t n, BHWorkspace &w, const BHEnsembleTables &
     if (err != cudaSuccess) return err;
     if (tm) tm->begin(kStageTraverse, st);
     const unsigned blocks = static_cast<unsigned>((static_cast<int64_t>(e.nwarps) * 32 + 255) / 256);
-    if (w.walk == kWalkGroup) {
-        if (w.counters)
-            group_walk_kernel<true, false, true, true><<<blocks, 256, 0, st>>>(
-                w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr, nullptr, w.counters, nullptr, 0, e.warps,
-                e.nwarps, e.params, w.P);
-        else if (e.all_soft)
-            group_walk_kernel<false, false, true, false><<<blocks, 256, 0, st>>>(
-                w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr, nullptr, nullptr, nullptr, 0, e.warps,
-                e.nwarps, e.params, w.P);
-        else
-            group_walk_kernel<false, false, true, true><<<blocks, 256, 0, st>>>(
-                w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr, nullptr, nullptr, nullptr, 0, e.warps,
-                e.nwarps, e.params, w.P);
-    } else if (w.counters)
-        traverse2_kernel<true, false, true, true><<<blocks, 256, 0, st>>>(w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P,
-                                                                          Vo, Ao, nullptr, nullptr, w.counters,
-                                                                          nullptr, 0, e.warps, e.nwarps, e.params, w.P);
+    if (w.counters)
+        launch_walk<true, false, true, true>(w, blocks, st, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr, nullptr,
+                                             w.counters, nullptr, 0, e.warps, e.nwarps, e.params, w.P);
     else if (e.all_soft)
-        traverse2_kernel<false, false, true, false><<<blocks, 256, 0, st>>>(
-            w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr, nullptr, nullptr, nullptr, 0, e.warps,
-            e.nwarps, e.params, w.P);
+        launch_walk<false, false, true, false>(w, blocks, st, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr,
+                                               nullptr, nullptr, nullptr, 0, e.warps, e.nwarps, e.params, w.P);
     else
-        traverse2_kernel<false, false, true, true><<<blocks, 256, 0, st>>>(
-            w.nodes, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr, nullptr, nullptr, nullptr, 0, e.warps,
-            e.nwarps, e.params, w.P);
+        launch_walk<false, false, true, true>(w, blocks, st, nullptr, Po, n, 0.f, 0.f, 0.f, P, Vo, Ao, nullptr, nullptr,
+                                              nullptr, nullptr, 0, e.warps, e.nwarps, e.params, w.P);
     if (tm) tm->end(kStageTraverse, st);
     return cudaGetLastError();
 }

@@ -51,8 +51,8 @@ struct SegView {
 
 // Walk forms over the same records (same accepted set per body).
 constexpr int kWalkUnion = 0;  // one record at a time for the warp's bodies, per-lane skip links
-constexpr int kWalkGroup = 1;  // records every body of the warp treats alike decided once for the
-                               // warp (summed densely), the union walk below the others
+constexpr int kWalkCell = 1;   // cell by cell: a cell's children decided side by side for the bodies
+                               // that opened it (from their box), per body only where they differ
 
 struct BHWorkspace {
     int64_t n = 0;
@@ -69,16 +69,17 @@ struct BHWorkspace {
     uint32_t *P = nullptr;  // n + 1 entries; P[n] = record count
     uint32_t *scan_sums = nullptr;
     BHNode *nodes = nullptr;  // up to 2n records
+    int *kids = nullptr;      // 8 child records per cell record (cell walk)
     // Traversal counters (pairwise evaluations, warp record visits): the
     // traversal counts into `counters` when it is set (= counter_mem).
     unsigned long long *counter_mem = nullptr;
     unsigned long long *counters = nullptr;
     int bodies_per_lane = 1;  // traversal shape: 1 or 2 bodies per lane
-    int walk = 1;             // with 2 bodies per lane: kWalkGroup or kWalkUnion
+    int walk = kWalkCell;     // with 2 bodies per lane: kWalkCell or kWalkUnion
     int64_t node_count_host = 0;
 };
 
-// The walk form: kWalkGroup, or kWalkUnion when NBODY_BH_WALK=union.
+// The walk form: kWalkCell, or kWalkUnion when NBODY_BH_WALK=union.
 int bh_walk_form();
 
 // Bytes of device memory for a workspace of n bodies, and its layout inside
