@@ -430,7 +430,8 @@ def bench_bh(args, world, rank, local, dist):
         stages[name] = st
     roofline = {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(fp32, 3), "unit": "TFLOP/s",
                 "frac": round(achieved / fp32, 4), "traffic": profile_traffic("bh_traverse"),
-                "kernel": "traverse2_kernel", "kernel_ms_per_launch": round(t_launch * 1e3, 4),
+                "kernel": "traverse2_kernel" if os.environ.get("NBODY_BH_WALK") == "union" else "cell_walk_kernel",
+                "kernel_ms_per_launch": round(t_launch * 1e3, 4),
                 "work": {"pair_evaluations_per_step": pairs, "per_body": round(pairs / n, 1),
                          "warp_record_visits_per_step": visits,
                          "pair_evaluations_per_warp_visit": round(pairs / max(1, visits), 2)},
@@ -457,10 +458,12 @@ def bench_bh(args, world, rank, local, dist):
     e2e = {"value": float(n) * e2e_steps * world / e2e_s, "unit": "body-steps/s", "h2d_bytes_per_step": 4 * 16 * n,
            "d2h_bytes_per_step": 4 * 16 * n, "ms_per_step": round(e2e_s * 1e3 / e2e_steps, 3), "steps": e2e_steps,
            "api": "nbody_update_host (ParticleSolver::updateParticlePositions)"}
-    # bbox, keys, sort (histogram, scan, 8 passes), gather, 8 build kernels, the
-    # upsweep (one climbing launch below 2^21 bodies; from there bucket centres,
-    # level count, level scatter and one launch per octree level: 24), walk
-    launches_per_step = 22 + (1 if n < (1 << 21) else 24)
+    # bbox, keys, sort (histogram, scan, 8 passes), gather, 8 build kernels and
+    # the child table of the cell walk, the upsweep (one climbing launch below
+    # 2^21 bodies; from there bucket centres, level count, level scatter and one
+    # launch per octree level: 24), walk
+    launches_per_step = 22 + (0 if os.environ.get("NBODY_BH_WALK") == "union" else 1) + \
+        (1 if n < (1 << 21) else 24)
     line = {"metric": METRIC, "component": "BH body-steps/s", "value": value, "unit": "body-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
