@@ -771,7 +771,9 @@ def bench_serving(args, world, rank, local, dist, rates=(10.0, 100.0, 1000.0), c
                                    f"ball R=100, N log-uniform in [1024, 4194304], steps U[10, 500], dt in "
                                    f"{{0.001, 0.0035}}, eps2 U[10, 40], theta=0.5; admission by HBM footprint under "
                                    f"150 GB; continuous batching in chunks of <= 10 steps, in 4 priority lanes by "
-                                   f"N x steps", "requests": count, "rates": list(rates), "crossover": X,
+                                   f"N x steps; Barnes-Hut requests of >= {serving.SOLO_N} bodies one at a time on "
+                                   f"the single-system solver in a fifth lane", "requests": count,
+                       "rates": list(rates), "crossover": X,
                        "pp_shape": shape, "body_steps_per_trace": int(body_steps), "parallelism": "replicas"},
             "p50_latency_s": head["served"]["p50_latency_s"], "p99_latency_s": head["served"]["p99_latency_s"],
             "plain_fifo": head["plain_fifo"], "speedup_vs_plain": head["speedup_sims_per_s"],

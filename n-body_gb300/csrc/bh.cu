@@ -1246,8 +1246,12 @@ __device__ __forceinline__ void add_record(const float4 cm, bool useA, bool useB
     }
 }
 
+// Five CTAs per SM (48 registers) for one system; an ensemble's form also
+// holds each system's eps^2 and theta^2 in registers and runs best at four
+// (64 registers, no spills): 2^21-body systems 0.93x the union walk's time
+// against 0.97x at five (GB300).
 template <bool COUNT, bool POT, bool SEG, bool GUARD>
-__global__ void __launch_bounds__(256, COUNT ? 4 : 5) cell_walk_kernel(
+__global__ void __launch_bounds__(256, (COUNT || SEG) ? 4 : 5) cell_walk_kernel(
     const BHNode *__restrict__ nodes, const int *__restrict__ kids, const uint32_t *__restrict__ node_total,
     const float4 *__restrict__ pos, int64_t n, float eps2, float theta2, float dt, float4 *__restrict__ pos_out,
     float4 *__restrict__ vel, float4 *__restrict__ acc, float4 *__restrict__ force_out, const int *__restrict__ ids,
@@ -1393,11 +1397,7 @@ __global__ void __launch_bounds__(256, COUNT ? 4 : 5) cell_walk_kernel(
         const unsigned bAmb = __ballot_sync(0xffffffffu, cls == 2);
         if (COUNT) n_visits += __popc(bAcc | bOpen | bAmb);
         const bool actA = (sa >> lane) & 1u, actB = (sb >> lane) & 1u;
-        for (unsigned m = bAcc; m; m &= m - 1) {
-            const int k = __shfl_sync(0xffffffffu, kid, __ffs(m) - 1);
-            add_record<COUNT, POT, GUARD>(__ldg(&nodes[k].cm), actA, actB, nx, ny, nz, e2, fx, fy, fz, phiA, phiB,
-                                          n_pairs);
-        }
+        // children opened by all are pushed first, so the box is dead during the sums below
         for (unsigned m = bOpen; m; m &= m - 1) {
             const int k = __shfl_sync(0xffffffffu, kid, __ffs(m) - 1);
             if (sp < kCellDepth) {
@@ -1412,6 +1412,11 @@ __global__ void __launch_bounds__(256, COUNT ? 4 : 5) cell_walk_kernel(
                 union_range<COUNT, POT, GUARD>(nodes, pos, n, k + 1, kend, actA, actB, nx, ny, nz, th, eps2, fx,
                                                fy, fz, phiA, phiB, n_pairs, n_visits);
             }
+        }
+        for (unsigned m = bAcc; m; m &= m - 1) {
+            const int k = __shfl_sync(0xffffffffu, kid, __ffs(m) - 1);
+            add_record<COUNT, POT, GUARD>(__ldg(&nodes[k].cm), actA, actB, nx, ny, nz, e2, fx, fy, fz, phiA, phiB,
+                                          n_pairs);
         }
         for (unsigned m = bAmb; m; m &= m - 1) decide(__shfl_sync(0xffffffffu, kid, __ffs(m) - 1), sa, sb);
     }

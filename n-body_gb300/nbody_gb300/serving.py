@@ -214,6 +214,25 @@ class Server:
 
 # Lane bounds in body-steps (N x steps) of a request's whole run.
 LANE_BOUNDS = (2e7, 2e8, 2e9)
+# Barnes-Hut requests from this size on run alone, one at a time, in a lane of
+# their own: one such system already fills the GPU (its walk has >= 16,384
+# warps), so batching it gains nothing, and the single-system solver's walk is
+# faster than the ensemble's on it (GB300, a 2^20 Plummer sphere: 4.6 against
+# 5.0 ms a step). Their results are the single-system solver's bit for bit.
+SOLO_N = 1 << 20
+
+
+class _Solo:
+    """The lane of the largest Barnes-Hut requests: one request at a time on
+    the single-system solver, stepped in chunks on the lane's stream."""
+
+    def __init__(self, stream):
+        self.stream = stream
+        self.incoming: list[tuple] = []  # (request, footprint, admitted at)
+        self.solver = None
+        self.active: _Active | None = None
+        self.event = None
+        self.chunk = 0
 
 
 class _Lane:
@@ -234,12 +253,14 @@ class LaneServer:
     with work has a chunk in flight, so lanes overlap on the GPU while the block
     scheduler favours the small ones; finished chunks are noticed by polling
     their events, their finished requests retired and arrivals admitted
-    (arrival order, shared memory budget). Results do not depend on lanes:
-    every system is computed on its own."""
+    (arrival order, shared memory budget). Barnes-Hut requests of solo_n
+    bodies or more run one at a time on the single-system solver in a lane of
+    their own, at the lowest priority, beside the batched lanes. Results do
+    not depend on lanes: every system is computed on its own."""
 
     def __init__(self, budget_bytes: float = 150e9, device: int = 0, crossover: int | None = None,
                  pp_shape: str | None = None, max_chunk: int = 10, keep_results: bool = True,
-                 bounds=LANE_BOUNDS):
+                 bounds=LANE_BOUNDS, solo_n: int | None = SOLO_N):
         import torch
 
         if crossover is None or pp_shape is None:
@@ -265,10 +286,18 @@ class LaneServer:
             ens = Ensemble(crossover=self.crossover, device=device, pp_shape=pp_shape)
             ens.set_stream(stream.cuda_stream)
             self.lanes.append(_Lane(k, ens, stream))
+        self.solo_n = None if solo_n is None else int(solo_n)
+        self.solo = _Solo(torch.cuda.Stream(device=device, priority=int(lo))) if self.solo_n else None
 
     def close(self) -> None:
         for lane in self.lanes:
             lane.ens.close()
+        if self.solo is not None and self.solo.solver is not None:
+            self.solo.solver.close()
+            self.solo.solver = None
+
+    def is_solo(self, req: Request) -> bool:
+        return self.solo is not None and req.n >= max(self.solo_n, self.crossover)
 
     def __enter__(self):
         return self
@@ -303,10 +332,39 @@ class LaneServer:
                                         admitted=a.admitted, completed=now())
             lane.ens.remove(a.sid)
 
-        while pending or queue or any(l.active or l.incoming for l in self.lanes):
+        solo = self.solo
+
+        def solo_end(err=None):
+            a = solo.active
+            system = None
+            if err is None and self.keep_results:
+                z = np.zeros((a.req.n, 4), np.float32)
+                system = ParticleSystem(z, z.copy(), np.zeros(a.req.n, np.float32), z.copy())
+                try:
+                    solo.solver.download(system, masses=True)
+                except NBodyError as e:
+                    err = str(e)
+            if solo.solver is not None:
+                solo.solver.close()
+            results[a.req.rid] = Result(a.req.rid, err is None, "bh", system if err is None else None,
+                                        error=err or "", arrival=a.req.arrival, admitted=a.admitted,
+                                        completed=now())
+            solo.solver, solo.active, solo.event = None, None, None
+            return a.footprint
+
+        def solo_busy():
+            return solo is not None and (solo.active is not None or solo.incoming)
+
+        while pending or queue or any(l.active or l.incoming for l in self.lanes) or solo_busy():
             t = now()
             while pending and (not realtime or pending[0].arrival <= t):
                 queue.append(pending.pop(0))
+            # the solo lane: a finished chunk moves its request on or retires it
+            if solo is not None and solo.event is not None and solo.event.query():
+                solo.event = None
+                solo.active.left -= solo.chunk
+                if solo.active.left <= 0:
+                    used -= solo_end()
             # retire lanes whose chunk has finished
             for lane in self.lanes:
                 if lane.event is None or not lane.event.query():
@@ -346,8 +404,39 @@ class LaneServer:
                 if used + fp > self.budget:
                     break
                 queue.pop(0)
-                self.lanes[self.lane_of(req)].incoming.append((req, fp, now()))
+                if self.is_solo(req):
+                    solo.incoming.append((req, fp, now()))
+                else:
+                    self.lanes[self.lane_of(req)].incoming.append((req, fp, now()))
                 used += fp
+            # the solo lane, when idle, starts its next request; one chunk at a time
+            if solo is not None and solo.event is None:
+                if solo.active is None and solo.incoming:
+                    req, fp, t_adm = solo.incoming.pop(0)
+                    solo.active = _Active(req, -1, req.steps, fp, t_adm, "bh")
+                    try:
+                        if req.init == "state" and (req.state is None or req.state.n != req.n):
+                            raise ValueError("request state missing or of the wrong size")
+                        solo.solver = ParticleSolverCUDA(req.dt, req.eps2, req.n, mode="bh", theta2=req.theta2,
+                                                         device=self.device)
+                        solo.solver.set_stream(solo.stream.cuda_stream)
+                        if req.init == "state":
+                            solo.solver.upload(req.state)
+                        else:
+                            solo.solver.init_device(req.init, seed=req.seed, params=req.params)
+                    except (NBodyError, ValueError) as e:
+                        used -= solo_end(str(e))
+                if solo.active is not None:
+                    k = min(self.max_chunk, solo.active.left)
+                    try:
+                        solo.solver.step(k)
+                        ev = torch.cuda.Event()
+                        ev.record(solo.stream)
+                        solo.event, solo.chunk = ev, k
+                        st.chunks += 1
+                        st.steps += k
+                    except NBodyError as e:
+                        used -= solo_end(str(e))
             # an idle lane takes its incoming requests, then every idle lane with
             # work launches a chunk
             launched = False
@@ -392,7 +481,7 @@ class LaneServer:
                 st.chunks += 1
                 st.steps += k
                 launched = True
-            in_flight = sum(len(l.active) for l in self.lanes)
+            in_flight = sum(len(l.active) for l in self.lanes) + (1 if solo is not None and solo.active else 0)
             st.max_in_flight = max(st.max_in_flight, in_flight)
             st.peak_footprint = max(st.peak_footprint, used)
             if not launched:

@@ -57,9 +57,12 @@ def test_served_results_equal_each_request_alone(nb, cuda):
         _same(one[r.rid].system, res[r.rid].system)
 
 
-def test_lane_server_results_equal_each_request_alone(nb, cuda):
+@pytest.mark.parametrize("solo_n", [None, 20_000])
+def test_lane_server_results_equal_each_request_alone(nb, cuda, solo_n):
     """Priority lanes (concurrent ensembles on streams of different priority)
-    give the same bits as the shared server, request by request."""
+    give the same bits as the shared server, request by request; so do the
+    largest Barnes-Hut requests run alone in the solo lane (the single-system
+    solver), here from 20,000 bodies on."""
     from nbody_gb300 import serving
 
     reqs = _trace(serving)
@@ -67,10 +70,13 @@ def test_lane_server_results_equal_each_request_alone(nb, cuda):
         shared = srv.run_trace(reqs, realtime=False)
     # bounds that spread this small trace over all four lanes
     with serving.LaneServer(budget_bytes=1e10, crossover=4096, pp_shape="128x2", max_chunk=3,
-                            bounds=(2e4, 1e5, 2e5)) as srv:
+                            bounds=(2e4, 1e5, 2e5), solo_n=solo_n) as srv:
         lanes = srv.run_trace(reqs, realtime=True)
-        used = {srv.lane_of(r) for r in reqs}
+        solo = [r for r in reqs if srv.is_solo(r)]
+        used = {srv.lane_of(r) for r in reqs if not srv.is_solo(r)}
         assert len(used) >= 3
+    if solo_n is not None:
+        assert len(solo) >= 2
     for r in reqs:
         assert lanes[r.rid].ok, lanes[r.rid].error
         _same(lanes[r.rid].system, shared[r.rid].system)
