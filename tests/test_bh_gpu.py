@@ -368,3 +368,29 @@ def test_bh_ten_steps_vs_port(nb, cuda, oracle):
     check_large(sysm.forces, fk)
     scale = np.abs(pk[:, :3]).max()
     assert np.abs(sysm.positions[:, :3] - pk[:, :3]).max() <= 1e-6 * scale
+
+
+@pytest.mark.parametrize("kind,n,eps2,theta2", [("plummer", 1 << 17, 40.0, 0.25), ("uniform_ball", 100_000, 40.0, 0.36),
+                                                ("plummer", 50_000, 0.0, 0.25)])
+def test_walk_forms_accept_the_same_pairs(nb, cuda, monkeypatch, kind, n, eps2, theta2):
+    """The cell walk (default) decides records for whole sets of bodies from
+    their box; the union walk decides every record body by body. Both must give
+    every body exactly the records its own reference walk accepts: the pair
+    counts of one step are equal, and the forces differ only by summation
+    order (eps^2 = 0 exercises the explicit zero-distance tests)."""
+    out = {}
+    for form in ("union", "cell"):
+        monkeypatch.setenv("NBODY_BH_WALK", form)
+        s = nb.ParticleSolverCUDA(0.0035, eps2, n, mode="bh", theta2=theta2)
+        s.init_device(kind, seed=77)
+        s.bh_counters(True)
+        s.step(1)
+        pairs, _ = s.bh_counters(False)
+        z = np.zeros((n, 4), np.float32)
+        sysm = nb.ParticleSystem(z.copy(), z.copy(), np.zeros(n, np.float32), z.copy())
+        s.download(sysm)
+        s.close()
+        out[form] = (pairs, sysm.forces.copy())
+    assert out["cell"][0] == out["union"][0] > 0
+    rms, mx = rel_err_stats(out["cell"][1], out["union"][1])
+    assert rms <= 1e-5 and mx <= 1e-3, (rms, mx)
