@@ -519,7 +519,7 @@ __global__ void emit_leaves_kernel(const uint64_t *__restrict__ k, int64_t n, co
 // has at most 8. Leaves and buckets get no entry. For the cell walk, which
 // decides a cell's children side by side.
 __global__ void kids_kernel(const BHNode *__restrict__ nodes, const uint32_t *__restrict__ total, int64_t cap,
-                            int *__restrict__ kids) {
+                            int *__restrict__ kids, int *status) {
     const int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const int64_t m = static_cast<int64_t>(*total) < cap ? static_cast<int64_t>(*total) : cap;
     if (r >= m) return;
@@ -537,6 +537,7 @@ __global__ void kids_kernel(const BHNode *__restrict__ nodes, const uint32_t *__
             c = nx > c ? nx : end;
         }
     }
+    if (c < end) record_error(status, NBODY_ERR_CAPACITY);  // more than 8 children: broken tree
     int4 *out = reinterpret_cast<int4 *>(kids + 8 * r);
     out[0] = make_int4(k[0], k[1], k[2], k[3]);
     out[1] = make_int4(k[4], k[5], k[6], k[7]);
@@ -1717,7 +1718,7 @@ cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaSt
                                                          !levels);
     if (w.walk == kWalkCell) {
         const int64_t cap = 2 * (n > 1 ? n : 2);
-        kids_kernel<<<grid_for(cap, 256), 256, 0, st>>>(w.nodes, w.P + n, cap, w.kids);
+        kids_kernel<<<grid_for(cap, 256), 256, 0, st>>>(w.nodes, w.P + n, cap, w.kids, status);
     }
     if (timer) timer->end(kStageBuild, st);
     if (timer) timer->begin(kStageUpsweep, st);
