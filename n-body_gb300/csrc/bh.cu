@@ -1183,8 +1183,8 @@ __device__ __forceinline__ int certify(const float4 cm, const int4 meta, const S
 // Same per-body acceptance as traverse2_kernel, organised by cells. A warp
 // holds a stack of cells that some of its bodies opened, each with the masks
 // of those bodies (first and second body of each lane) and their box. For a
-// cell popped, eight lanes load its children and decide each one for the
-// whole set from the box (certify: accepted by all of them, opened by all of
+// cell popped (up to four at a time), eight lanes load its children and
+// decide each one for the whole set from the box (certify: accepted by all of them, opened by all of
 // them, or ambiguous). Accepted children are summed by those bodies with no
 // criterion; children opened by all are pushed with the same set and box;
 // each ambiguous child gets the per-body criterion, its accepting bodies sum
@@ -1261,12 +1261,18 @@ __global__ void __launch_bounds__(256, (COUNT || SEG) ? 4 : 5) cell_walk_kernel(
     __shared__ int4 stk_i[kCellWarps][kCellDepth];     // cell, mask A, mask B, -
     __shared__ float4 stk_lo[kCellWarps][kCellDepth];  // box: lx, ly, lz, hx
     __shared__ float2 stk_hi[kCellWarps][kCellDepth];  // box: hy, hz
+    __shared__ int4 bat_i[kCellWarps][4];                // the cells of a round, as popped
+    __shared__ float4 bat_lo[kCellWarps][4];
+    __shared__ float2 bat_hi[kCellWarps][4];
     unsigned long long n_pairs = 0, n_visits = 0;
     float phiA = 0.f, phiB = 0.f;
     const int lane = threadIdx.x & 31;
     int4 *si = stk_i[threadIdx.x >> 5];
     float4 *slo = stk_lo[threadIdx.x >> 5];
     float2 *shi = stk_hi[threadIdx.x >> 5];
+    int4 *bi = bat_i[threadIdx.x >> 5];
+    float4 *blo = bat_lo[threadIdx.x >> 5];
+    float2 *bhi = bat_hi[threadIdx.x >> 5];
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     int64_t base, end;
     int root, rend;
@@ -1371,55 +1377,66 @@ __global__ void __launch_bounds__(256, (COUNT || SEG) ? 4 : 5) cell_walk_kernel(
     };
 
     if (root < rend) decide(root, __ballot_sync(0xffffffffu, vA), __ballot_sync(0xffffffffu, vB));
+    // Up to four cells per round: lanes 8g .. 8g + 7 take the children of cell
+    // g and decide them for its set; the popped entries move to a batch area
+    // that the round's pushes cannot reach.
+    const int grp = lane >> 3;
     while (sp > 0) {
-        --sp;
-        __syncwarp();  // lane 0's writes of the entry before every lane reads it
-        const int4 t = si[sp];
-        const float4 bl = slo[sp];
-        const float2 bh = shi[sp];
-        __syncwarp();  // every lane has read the entry before the slot is written again
-        const int c = t.x;
-        const unsigned sa = static_cast<unsigned>(t.y), sb = static_cast<unsigned>(t.z);
-        SetBox box;
-        box.lx = bl.x;
-        box.ly = bl.y;
-        box.lz = bl.z;
-        box.hx = bl.w;
-        box.hy = bh.x;
-        box.hz = bh.y;
-        // eight lanes take the cell's children and decide them for the whole set
+        const int nb = sp < 4 ? sp : 4;
+        sp -= nb;
+        __syncwarp();  // lane 0's writes of the entries before the lanes read them
         int kid = -1, cls = 3;
-        if (lane < 8) {
-            kid = __ldg(&kids[8 * static_cast<int64_t>(c) + lane]);
+        if (grp < nb) {
+            const int4 t = si[sp + grp];
+            const float4 bl = slo[sp + grp];
+            const float2 bh = shi[sp + grp];
+            if ((lane & 7) == 0) {
+                bi[grp] = t;
+                blo[grp] = bl;
+                bhi[grp] = bh;
+            }
+            SetBox box;
+            box.lx = bl.x;
+            box.ly = bl.y;
+            box.lz = bl.z;
+            box.hx = bl.w;
+            box.hy = bh.x;
+            box.hz = bh.y;
+            kid = __ldg(&kids[8 * static_cast<int64_t>(t.x) + (lane & 7)]);
             if (kid >= 0) cls = certify(__ldg(&nodes[kid].cm), __ldg(&nodes[kid].meta), box, theta2);
         }
+        __syncwarp();  // the batch written, and the popped slots read, before pushes reuse them
         const unsigned bAcc = __ballot_sync(0xffffffffu, cls == 0);
         const unsigned bOpen = __ballot_sync(0xffffffffu, cls == 1);
         const unsigned bAmb = __ballot_sync(0xffffffffu, cls == 2);
         if (COUNT) n_visits += __popc(bAcc | bOpen | bAmb);
-        const bool actA = (sa >> lane) & 1u, actB = (sb >> lane) & 1u;
-        // children opened by all are pushed first, so the box is dead during the sums below
-        for (unsigned m = bOpen; m; m &= m - 1) {
-            const int k = __shfl_sync(0xffffffffu, kid, __ffs(m) - 1);
-            if (sp < kCellDepth) {
-                if (lane == 0) {
-                    si[sp] = make_int4(k, static_cast<int>(sa), static_cast<int>(sb), 0);
-                    slo[sp] = bl;
-                    shi[sp] = bh;
+        for (int q = 0; q < nb; ++q) {
+            const unsigned gm = 0xffu << (8 * q);
+            const int4 t = bi[q];
+            const unsigned sa = static_cast<unsigned>(t.y), sb = static_cast<unsigned>(t.z);
+            const bool actA = (sa >> lane) & 1u, actB = (sb >> lane) & 1u;
+            for (unsigned m = bOpen & gm; m; m &= m - 1) {
+                const int k = __shfl_sync(0xffffffffu, kid, __ffs(m) - 1);
+                if (sp < kCellDepth) {
+                    if (lane == 0) {
+                        si[sp] = make_int4(k, static_cast<int>(sa), static_cast<int>(sb), 0);
+                        slo[sp] = blo[q];
+                        shi[sp] = bhi[q];
+                    }
+                    ++sp;
+                } else {
+                    const int kend = __ldg(&nodes[k].meta).y;
+                    union_range<COUNT, POT, GUARD>(nodes, pos, n, k + 1, kend, actA, actB, nx, ny, nz, th, eps2, fx,
+                                                   fy, fz, phiA, phiB, n_pairs, n_visits);
                 }
-                ++sp;
-            } else {
-                const int kend = __ldg(&nodes[k].meta).y;
-                union_range<COUNT, POT, GUARD>(nodes, pos, n, k + 1, kend, actA, actB, nx, ny, nz, th, eps2, fx,
-                                               fy, fz, phiA, phiB, n_pairs, n_visits);
             }
+            for (unsigned m = bAcc & gm; m; m &= m - 1) {
+                const int k = __shfl_sync(0xffffffffu, kid, __ffs(m) - 1);
+                add_record<COUNT, POT, GUARD>(__ldg(&nodes[k].cm), actA, actB, nx, ny, nz, e2, fx, fy, fz, phiA,
+                                              phiB, n_pairs);
+            }
+            for (unsigned m = bAmb & gm; m; m &= m - 1) decide(__shfl_sync(0xffffffffu, kid, __ffs(m) - 1), sa, sb);
         }
-        for (unsigned m = bAcc; m; m &= m - 1) {
-            const int k = __shfl_sync(0xffffffffu, kid, __ffs(m) - 1);
-            add_record<COUNT, POT, GUARD>(__ldg(&nodes[k].cm), actA, actB, nx, ny, nz, e2, fx, fy, fz, phiA, phiB,
-                                          n_pairs);
-        }
-        for (unsigned m = bAmb; m; m &= m - 1) decide(__shfl_sync(0xffffffffu, kid, __ffs(m) - 1), sa, sb);
     }
 
     if (COUNT) {
