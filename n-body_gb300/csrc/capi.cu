@@ -63,6 +63,9 @@ struct nbody_ctx {
     // Diagnostics: reduction scratch, 8 doubles of output, per-body potential.
     void *diag_mem = nullptr;
     float *diag_phi = nullptr;
+    // Side stream and events of the overlapped host step (made on first use).
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace {
@@ -184,7 +187,10 @@ int ensure_workspace(nbody_ctx *ctx, int64_t n) {
 }
 
 // One Barnes-Hut step on the resident state (see nbody_ctx for the layout).
-int bh_step(nbody_ctx *ctx) {
+// join: when set, the step waits for it before its gather and first merges
+// the masses in `masses4` (device, reference layout) into the positions,
+// which were copied in with w = 0 (the overlapped host step).
+int bh_step(nbody_ctx *ctx, cudaEvent_t join = nullptr, const float4 *masses4 = nullptr) {
     nbody::BHWorkspace &w = ctx->ws;
     const int64_t n = ctx->n;
     float4 *P = ctx->pos[ctx->bh_pos], *Po = ctx->pos[ctx->bh_pos ^ 1];
@@ -196,6 +202,10 @@ int bh_step(nbody_ctx *ctx) {
     NB_CK(ctx, nbody::bh_bbox(P, n, w, ctx->stream, tm));
     NB_CK(ctx, nbody::bh_keys(P, n, w, ctx->key_mode, ctx->stream, tm));
     NB_CK(ctx, nbody::bh_sort(n, w, ctx->stream, ctx->status, tm));
+    if (join) {
+        NB_CK(ctx, cudaStreamWaitEvent(ctx->stream, join, 0));
+        NB_CK(ctx, nbody::merge_masses(P, masses4, n, ctx->stream));
+    }
     NB_CK(ctx, nbody::bh_gather(n, w, P, V, A, I, Po, Vo, Ao, Io, ctx->stream, ctx->status, tm));
     NB_CK(ctx, nbody::bh_build(Po, n, w, ctx->stream, ctx->status, tm));
     // New positions go to the buffer the gather just read from.
@@ -313,6 +323,9 @@ int nbody_destroy(nbody_ctx *ctx) {
         cudaFree(ctx->diag_mem);
         cudaFree(ctx->diag_phi);
         delete ctx->timer;
+        if (ctx->side) cudaStreamDestroy(ctx->side);
+        if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+        if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
         if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     }
     delete ctx;
@@ -453,9 +466,58 @@ int nbody_host_in_place(const void *p, int64_t bytes, int device) {
     return nbody::host_mapped(p, static_cast<size_t>(bytes), device) ? 1 : 0;
 }
 
+namespace {
+
+// nbody_update_host for Barnes-Hut with page-locked host arrays: positions come
+// in first by a DMA copy (the reference layout's w = 0), velocities,
+// accelerations and masses by DMA copies on a side stream while the first
+// step's box, keys and sort run on the SMs; the step merges the masses into
+// the positions just before its gather, the first use of any of them. Same
+// values as nbody_upload + nbody_step.
+int bh_update_overlapped(nbody_ctx *ctx, const float *positions4, const float *velocities4,
+                         const float *accelerations4, const float *masses4, int steps) {
+    DeviceGuard dg(ctx->device);
+    int rc = ensure_workspace(ctx, ctx->n);
+    if (rc != NBODY_OK) return rc;
+    if (!ctx->side) {
+        NB_CK(ctx, cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+        NB_CK(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+        NB_CK(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+    }
+    const size_t b4 = static_cast<size_t>(ctx->n) * sizeof(float4);
+    NB_CK(ctx, cudaEventRecord(ctx->ev_fork, ctx->stream));
+    NB_CK(ctx, cudaMemcpyAsync(ctx->pos[0], positions4, b4, cudaMemcpyHostToDevice, ctx->stream));
+    NB_CK(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+    NB_CK(ctx, cudaMemcpyAsync(ctx->vel, velocities4, b4, cudaMemcpyHostToDevice, ctx->side));
+    NB_CK(ctx, cudaMemcpyAsync(ctx->acc, accelerations4, b4, cudaMemcpyHostToDevice, ctx->side));
+    NB_CK(ctx, cudaMemcpyAsync(ctx->stage, masses4, b4, cudaMemcpyHostToDevice, ctx->side));
+    NB_CK(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
+    ctx->cur = 0;
+    ctx->bh_pos = 0;
+    ctx->bh_va = 0;
+    ctx->ids_valid = false;
+    ctx->uploaded = true;
+    rc = bh_step(ctx, ctx->ev_join, ctx->stage);
+    if (rc == NBODY_OK) rc = bh_steps(ctx, steps - 1);
+    return rc;
+}
+
+}  // namespace
+
 int nbody_update_host(nbody_ctx *ctx, float *positions4, float *velocities4, float *accelerations4,
                       const float *masses4, float *forces4, int steps) {
     if (!ctx || !positions4 || !velocities4 || !accelerations4 || !masses4 || steps < 0) return NBODY_ERR_ARG;
+    if (ctx->mode == NBODY_MODE_BH && steps >= 1) {
+        const size_t b4 = static_cast<size_t>(ctx->n) * sizeof(float4);
+        const int dev = ctx->device;
+        DeviceGuard dg(dev);
+        if (nbody::host_mapped(positions4, b4, dev) && nbody::host_mapped(velocities4, b4, dev) &&
+            nbody::host_mapped(accelerations4, b4, dev) && nbody::host_mapped(masses4, b4, dev)) {
+            int rc = bh_update_overlapped(ctx, positions4, velocities4, accelerations4, masses4, steps);
+            if (rc == NBODY_OK) rc = nbody_download(ctx, positions4, velocities4, accelerations4, forces4);
+            return rc;
+        }
+    }
     int rc = nbody_upload(ctx, positions4, velocities4, accelerations4, masses4);
     if (rc == NBODY_OK) rc = nbody_step(ctx, steps);
     if (rc == NBODY_OK) rc = nbody_download(ctx, positions4, velocities4, accelerations4, forces4);

@@ -40,6 +40,14 @@ __global__ void invert_ids_kernel(const int *__restrict__ ids, int *__restrict__
     inv[d] = static_cast<int>(i);
 }
 
+// pos_mass[i].w = masses4[i].x: the masses of the reference layout (brought in
+// by a copy) merged into positions copied with w = 0.
+__global__ void merge_masses_kernel(float4 *__restrict__ pos_mass, const float4 *__restrict__ masses4, int64_t n) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    pos_mass[i].w = masses4[i].x;
+}
+
 // Device state -> the caller's arrays, walking the caller's order d so that
 // the writes into host memory are contiguous: body d is state row inv[d] (or
 // d without inv). Positions leave with w = 0, masses in the reference's vec4
@@ -125,6 +133,14 @@ float4 *host_mapped(const void *p, size_t bytes, int device) {
         !range_holds(reinterpret_cast<uintptr_t>(a.devicePointer), bytes))
         return nullptr;
     return static_cast<float4 *>(a.devicePointer);
+}
+
+cudaError_t merge_masses(float4 *pos_mass, const float4 *masses4, int64_t n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    merge_masses_kernel<<<static_cast<unsigned>((n + threads - 1) / threads), threads, 0, stream>>>(pos_mass, masses4,
+                                                                                                   n);
+    return cudaGetLastError();
 }
 
 cudaError_t host_gather(const float4 *positions4, const float4 *masses4, const float4 *vel_h, const float4 *acc_h,

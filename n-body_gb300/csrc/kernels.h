@@ -81,6 +81,8 @@ cudaError_t unpack_masses(const float4 *pos_mass, const int *ids, float4 *masses
 // device's page-locked memory, a range shorter than `bytes`, or not 16-byte
 // aligned).
 float4 *host_mapped(const void *p, size_t bytes, int device);
+// pos_mass[i].w = masses4[i].x (device arrays).
+cudaError_t merge_masses(float4 *pos_mass, const float4 *masses4, int64_t n, cudaStream_t stream);
 cudaError_t host_gather(const float4 *positions4, const float4 *masses4, const float4 *vel_h, const float4 *acc_h,
                         float4 *pos_mass, float4 *vel, float4 *acc, int64_t n, cudaStream_t stream);
 cudaError_t host_scatter(const float4 *pos_mass, const float4 *vel, const float4 *acc, const int *ids, int *inv,
