@@ -1192,7 +1192,7 @@ __device__ __forceinline__ int certify(const float4 cm, const int4 meta, const S
 // bodies, and the bodies that open a plain cell are pushed with it as a new,
 // smaller set with its own box. A body thus meets exactly the records of its
 // own reference walk, and decides by itself only those its set disagrees on.
-constexpr int kCellWarps = 8;   // 256-thread CTAs
+constexpr int kCellWarps = 2;   // 64-thread CTAs: finer blocks shorten the grid's uneven last wave
 constexpr int kCellDepth = 48;  // stack entries per warp; a full stack sends a cell to union_range
 
 // Box of the bodies in masks sa / sb (exact min / max on the order-preserving
@@ -1247,12 +1247,13 @@ __device__ __forceinline__ void add_record(const float4 cm, bool useA, bool useB
     }
 }
 
-// Five CTAs per SM (48 registers) for one system; an ensemble's form also
-// holds each system's eps^2 and theta^2 in registers and runs best at four
-// (64 registers, no spills): 2^21-body systems 0.93x the union walk's time
-// against 0.97x at five (GB300).
+// 64-thread CTAs, twenty per SM (48 registers) for one system; an ensemble's
+// form also holds each system's eps^2 and theta^2 in registers and runs best
+// at sixteen (64 registers, no spills). Against 256-thread CTAs at the same
+// occupancy the finer blocks shorten the uneven last wave: 4.19 vs 4.28 ms at
+// 2^20, 30.8 vs 31.5 ms for a 512-system ensemble (GB300).
 template <bool COUNT, bool POT, bool SEG, bool GUARD>
-__global__ void __launch_bounds__(256, (COUNT || SEG) ? 4 : 5) cell_walk_kernel(
+__global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 20) cell_walk_kernel(
     const BHNode *__restrict__ nodes, const int *__restrict__ kids, const uint32_t *__restrict__ node_total,
     const float4 *__restrict__ pos, int64_t n, float eps2, float theta2, float dt, float4 *__restrict__ pos_out,
     float4 *__restrict__ vel, float4 *__restrict__ acc, float4 *__restrict__ force_out, const int *__restrict__ ids,
@@ -1767,7 +1768,7 @@ void launch_walk(const BHWorkspace &w, unsigned blocks, cudaStream_t st, const u
                  float4 *acc, float4 *force_out, const int *ids, unsigned long long *counters, float *phi_out,
                  int euler, const int4 *work, int nwork, const float4 *params, const uint32_t *P) {
     if (w.walk == kWalkCell)
-        cell_walk_kernel<COUNT, POT, SEG, GUARD><<<blocks, 256, 0, st>>>(w.nodes, w.kids, node_total, pos, n, eps2,
+        cell_walk_kernel<COUNT, POT, SEG, GUARD><<<blocks * 4, 64, 0, st>>>(w.nodes, w.kids, node_total, pos, n, eps2,
                                                                          theta2, dt, pos_out, vel, acc, force_out,
                                                                          ids, counters, phi_out, euler, work, nwork,
                                                                          params, P);
