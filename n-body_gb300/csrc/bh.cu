@@ -1247,13 +1247,15 @@ __device__ __forceinline__ void add_record(const float4 cm, bool useA, bool useB
     }
 }
 
-// 64-thread CTAs, twenty per SM (48 registers) for one system; an ensemble's
+// 64-thread CTAs. One system: twenty-four per SM (40 registers, 48 warps):
+// 4.05 ms at 2^20 against 4.18 at twenty (48 registers) and 4.21 at
+// twenty-eight or thirty-two, 14.4 vs 15.4 ms at 4M (GB300). An ensemble's
 // form also holds each system's eps^2 and theta^2 in registers and runs best
-// at sixteen (64 registers, no spills). Against 256-thread CTAs at the same
-// occupancy the finer blocks shorten the uneven last wave: 4.19 vs 4.28 ms at
-// 2^20, 30.8 vs 31.5 ms for a 512-system ensemble (GB300).
+// at sixteen (64 registers, no spills; 33.7 vs 30.8 ms at twenty for a
+// 512-system ensemble). Against 256-thread CTAs at the same occupancy the
+// finer blocks shorten the uneven last wave (4.19 vs 4.28 ms at 2^20).
 template <bool COUNT, bool POT, bool SEG, bool GUARD>
-__global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 20) cell_walk_kernel(
+__global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel(
     const BHNode *__restrict__ nodes, const int *__restrict__ kids, const uint32_t *__restrict__ node_total,
     const float4 *__restrict__ pos, int64_t n, float eps2, float theta2, float dt, float4 *__restrict__ pos_out,
     float4 *__restrict__ vel, float4 *__restrict__ acc, float4 *__restrict__ force_out, const int *__restrict__ ids,
