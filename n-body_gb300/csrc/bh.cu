@@ -1,7 +1,10 @@
 // Barnes-Hut gravity for sm_103a: per-step bounding box, 63-bit Morton keys,
 // stable radix sort, state gather, octree from sorted keys, bottom-up mass /
-// centre of mass, and a warp-cooperative stackless traversal with the
-// reference's opening criterion and integrator fused in.
+// centre of mass, and a warp-cooperative walk with the reference's opening
+// criterion and integrator fused in: by default the cell walk (a cell's
+// children decided for whole sets of bodies from their box, body by body only
+// where the set disagrees), or the stackless union walk (NBODY_BH_WALK=union);
+// both give every body exactly the records its own reference walk accepts.
 //
 // Replaces the reference's -v 6 CPU path (ParticleSolverBHutCPUParallel,
 // src/ParticleSolver/ParticleSolverBHutCPUParallel/ParticleSolverBHutCPUParallel.cpp:18-41
