@@ -1188,8 +1188,10 @@ __device__ __forceinline__ int certify(const float4 cm, const int4 meta, const S
 // of those bodies (first and second body of each lane) and their box. For a
 // cell popped (up to four at a time), eight lanes load its children and
 // decide each one for the whole set from the box (certify: accepted by all of them, opened by all of
-// them, or ambiguous). Accepted children are summed by those bodies with no
-// criterion; children opened by all are pushed with the same set and box;
+// them, or ambiguous) while leaving its cm in shared memory. Accepted
+// children are summed by those bodies with no criterion, in batches read from
+// shared memory (3.51 against 4.05 ms at 2^20 when each was fetched on its own
+// by record index); children opened by all are pushed with the same set and box;
 // each ambiguous child gets the per-body criterion, its accepting bodies sum
 // it (or a bucket's bodies), the bodies that open a terminal cell sum its
 // bodies, and the bodies that open a plain cell are pushed with it as a new,
@@ -1252,7 +1254,9 @@ __device__ __forceinline__ void add_record(const float4 cm, bool useA, bool useB
 
 // 64-thread CTAs. One system: twenty-four per SM (40 registers, 48 warps):
 // 4.05 ms at 2^20 against 4.18 at twenty (48 registers) and 4.21 at
-// twenty-eight or thirty-two, 14.4 vs 15.4 ms at 4M (GB300). An ensemble's
+// twenty-eight or thirty-two, 14.4 vs 15.4 ms at 4M (GB300, before the
+// children's cm moved to shared memory; with them there twenty still loses,
+// 4.0 vs 3.67 ms). An ensemble's
 // form also holds each system's eps^2 and theta^2 in registers and runs best
 // at sixteen (64 registers, no spills; 33.7 vs 30.8 ms at twenty for a
 // 512-system ensemble). Against 256-thread CTAs at the same occupancy the
@@ -1270,6 +1274,7 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
     __shared__ int4 bat_i[kCellWarps][4];                // the cells of a round, as popped
     __shared__ float4 bat_lo[kCellWarps][4];
     __shared__ float2 bat_hi[kCellWarps][4];
+    __shared__ float4 ch_cm[kCellWarps][32];             // the round's children's cm, by the lane that loaded them
     unsigned long long n_pairs = 0, n_visits = 0;
     float phiA = 0.f, phiB = 0.f;
     const int lane = threadIdx.x & 31;
@@ -1279,6 +1284,7 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
     int4 *bi = bat_i[threadIdx.x >> 5];
     float4 *blo = bat_lo[threadIdx.x >> 5];
     float2 *bhi = bat_hi[threadIdx.x >> 5];
+    float4 *ccm = ch_cm[threadIdx.x >> 5];
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     int64_t base, end;
     int root, rend;
@@ -1311,9 +1317,7 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
     // Record k decided body by body for the bodies in (sa, sb); the bodies
     // that open a plain cell are pushed with it (or, on a full stack, walk
     // its subtree with union_range).
-    auto decide = [&](int k, unsigned sa, unsigned sb) {
-        const float4 cm = __ldg(&nodes[k].cm);
-        const int4 meta = __ldg(&nodes[k].meta);
+    auto decide = [&](int k, const float4 cm, const int4 meta, unsigned sa, unsigned sb) {
         const bool actA = (sa >> lane) & 1u, actB = (sb >> lane) & 1u;
         const float2 dx = __fadd2_rn(make_float2(cm.x, cm.x), nx);
         const float2 dy = __fadd2_rn(make_float2(cm.y, cm.y), ny);
@@ -1382,11 +1386,17 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
         }
     };
 
-    if (root < rend) decide(root, __ballot_sync(0xffffffffu, vA), __ballot_sync(0xffffffffu, vB));
+    if (root < rend)
+        decide(root, __ldg(&nodes[root].cm), __ldg(&nodes[root].meta), __ballot_sync(0xffffffffu, vA),
+               __ballot_sync(0xffffffffu, vB));
     // Up to four cells per round: lanes 8g .. 8g + 7 take the children of cell
     // g and decide them for its set; the popped entries move to a batch area
     // that the round's pushes cannot reach.
     const int grp = lane >> 3;
+    // Accepted children summed per batch: eight for one system (3.51 vs 3.58
+    // ms at four, 2^20 Plummer), four for ensembles (28.9 vs 29.5 ms, 512
+    // systems), whose form holds more registers.
+    constexpr int kBatch = SEG ? 4 : 8;
     while (sp > 0) {
         const int nb = sp < 4 ? sp : 4;
         sp -= nb;
@@ -1409,7 +1419,11 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
             box.hy = bh.x;
             box.hz = bh.y;
             kid = __ldg(&kids[8 * static_cast<int64_t>(t.x) + (lane & 7)]);
-            if (kid >= 0) cls = certify(__ldg(&nodes[kid].cm), __ldg(&nodes[kid].meta), box, theta2);
+            if (kid >= 0) {
+                const float4 cm = __ldg(&nodes[kid].cm);
+                ccm[lane] = cm;
+                cls = certify(cm, __ldg(&nodes[kid].meta), box, theta2);
+            }
         }
         __syncwarp();  // the batch written, and the popped slots read, before pushes reuse them
         const unsigned bAcc = __ballot_sync(0xffffffffu, cls == 0);
@@ -1436,12 +1450,29 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
                                                    fy, fz, phiA, phiB, n_pairs, n_visits);
                 }
             }
-            for (unsigned m = bAcc & gm; m; m &= m - 1) {
-                const int k = __shfl_sync(0xffffffffu, kid, __ffs(m) - 1);
-                add_record<COUNT, POT, GUARD>(__ldg(&nodes[k].cm), actA, actB, nx, ny, nz, e2, fx, fy, fz, phiA,
-                                              phiB, n_pairs);
+            // Accepted children in batches: their cm come from shared memory
+            // (bit c of the mask is lane c's child), all loads of a batch
+            // before its sums.
+            unsigned m = bAcc & gm;
+            while (__popc(m) >= kBatch) {
+                float4 c[kBatch];
+#pragma unroll
+                for (int j = 0; j < kBatch; ++j) {
+                    c[j] = ccm[__ffs(m) - 1];
+                    m &= m - 1;
+                }
+#pragma unroll
+                for (int j = 0; j < kBatch; ++j)
+                    add_record<COUNT, POT, GUARD>(c[j], actA, actB, nx, ny, nz, e2, fx, fy, fz, phiA, phiB, n_pairs);
             }
-            for (unsigned m = bAmb & gm; m; m &= m - 1) decide(__shfl_sync(0xffffffffu, kid, __ffs(m) - 1), sa, sb);
+            for (; m; m &= m - 1)
+                add_record<COUNT, POT, GUARD>(ccm[__ffs(m) - 1], actA, actB, nx, ny, nz, e2, fx, fy, fz, phiA, phiB,
+                                              n_pairs);
+            for (m = bAmb & gm; m; m &= m - 1) {
+                const int c = __ffs(m) - 1;
+                const int k = __shfl_sync(0xffffffffu, kid, c);
+                decide(k, ccm[c], __ldg(&nodes[k].meta), sa, sb);
+            }
         }
     }
 
