@@ -1268,23 +1268,28 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
     float4 *__restrict__ vel, float4 *__restrict__ acc, float4 *__restrict__ force_out, const int *__restrict__ ids,
     unsigned long long *__restrict__ counters, float *__restrict__ phi_out, int euler, const int4 *__restrict__ work,
     int nwork, const float4 *__restrict__ params, const uint32_t *__restrict__ P) {
-    __shared__ int4 stk_i[kCellWarps][kCellDepth];     // cell, mask A, mask B, -
-    __shared__ float4 stk_lo[kCellWarps][kCellDepth];  // box: lx, ly, lz, hx
-    __shared__ float2 stk_hi[kCellWarps][kCellDepth];  // box: hy, hz
-    __shared__ int4 bat_i[kCellWarps][4];                // the cells of a round, as popped
-    __shared__ float4 bat_lo[kCellWarps][4];
-    __shared__ float2 bat_hi[kCellWarps][4];
-    __shared__ float4 ch_cm[kCellWarps][32];             // the round's children's cm, by the lane that loaded them
+    // One block of shared memory per warp, addressed from one base.
+    struct __align__(16) WarpArea {
+        int4 stk_i[kCellDepth];     // cell, mask A, mask B, -
+        float4 stk_lo[kCellDepth];  // box: lx, ly, lz, hx
+        float2 stk_hi[kCellDepth];  // box: hy, hz
+        int4 bat_i[4];              // the cells of a round, as popped
+        float4 bat_lo[4];
+        float2 bat_hi[4];
+        float4 ch_cm[32];           // the round's children's cm, by the lane that loaded them
+    };
+    __shared__ WarpArea area[kCellWarps];
+    WarpArea &A = area[threadIdx.x >> 5];
     unsigned long long n_pairs = 0, n_visits = 0;
     float phiA = 0.f, phiB = 0.f;
     const int lane = threadIdx.x & 31;
-    int4 *si = stk_i[threadIdx.x >> 5];
-    float4 *slo = stk_lo[threadIdx.x >> 5];
-    float2 *shi = stk_hi[threadIdx.x >> 5];
-    int4 *bi = bat_i[threadIdx.x >> 5];
-    float4 *blo = bat_lo[threadIdx.x >> 5];
-    float2 *bhi = bat_hi[threadIdx.x >> 5];
-    float4 *ccm = ch_cm[threadIdx.x >> 5];
+    int4 *si = A.stk_i;
+    float4 *slo = A.stk_lo;
+    float2 *shi = A.stk_hi;
+    int4 *bi = A.bat_i;
+    float4 *blo = A.bat_lo;
+    float2 *bhi = A.bat_hi;
+    float4 *ccm = A.ch_cm;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     int64_t base, end;
     int root, rend;
