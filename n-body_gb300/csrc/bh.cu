@@ -815,7 +815,8 @@ __device__ __forceinline__ void direct_sum_range2(const float4 *__restrict__ pos
 __device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, float fy, float fz, float dt,
                                                  float4 *__restrict__ pos_out, float4 *__restrict__ vel,
                                                  float4 *__restrict__ acc, float4 *__restrict__ force_out,
-                                                 const int *__restrict__ ids, int64_t n, int euler);
+                                                 const int *__restrict__ ids, int64_t n, int euler,
+                                                 const HostOut &host = HostOut{});
 
 // COUNT adds up (per warp, one atomic each) the pairwise force evaluations
 // and the records the warp visited; used for measurement only.
@@ -931,14 +932,28 @@ __device__ __forceinline__ void direct_sum_range(const float4 *__restrict__ pos,
     }
 }
 
+// Body b's new state into the caller's arrays at its caller index (kept out
+// of line: inlined, its loads were hoisted into the walk and spilled there).
+__device__ __noinline__ void write_host(const HostOut host, const int *__restrict__ ids, int64_t b, int64_t n,
+                                        float4 p, float4 v, float4 a) {
+    const int d = ids ? ids[b] : static_cast<int>(b);
+    if (d < 0 || d >= n) return;
+    host.pos[d] = make_float4(p.x, p.y, p.z, 0.f);
+    host.vel[d] = v;
+    host.acc[d] = a;
+    if (host.force) host.force[d] = a;
+}
+
 __device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, float fy, float fz, float dt,
                                                  float4 *__restrict__ pos_out, float4 *__restrict__ vel,
                                                  float4 *__restrict__ acc, float4 *__restrict__ force_out,
-                                                 const int *__restrict__ ids, int64_t n, int euler) {
+                                                 const int *__restrict__ ids, int64_t n, int euler,
+                                                 const HostOut &host) {
     const float4 anew = make_float4(fx, fy, fz, 0.f);
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
     if (pos_out && euler) {
         // updateParticles.glsl:44-55: v += F dt, then x += v dt.
-        float4 v = vel[b];
+        v = vel[b];
         v.x = __fadd_rn(v.x, __fmul_rn(fx, dt));
         v.y = __fadd_rn(v.y, __fmul_rn(fy, dt));
         v.z = __fadd_rn(v.z, __fmul_rn(fz, dt));
@@ -951,7 +966,7 @@ __device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, 
     } else if (pos_out) {
         // Reference integrator (include/ParticleSystem.h:52-69), no contraction.
         const float h = __fmul_rn(dt, 0.5f);
-        float4 v = vel[b];
+        v = vel[b];
         const float4 a = acc[b];
         v.x = __fadd_rn(v.x, __fmul_rn(a.x, h));
         v.y = __fadd_rn(v.y, __fmul_rn(a.y, h));
@@ -970,6 +985,7 @@ __device__ __forceinline__ void integrate_sorted(int64_t b, float4 p, float fx, 
         const int d = ids ? ids[b] : static_cast<int>(b);
         if (d >= 0 && d < n) force_out[d] = anew;
     }
+    if (host.pos && pos_out) write_host(host, ids, b, n, p, v, anew);
 }
 
 // The union walk over the records [i, iend) (the whole tree, or the subtree
@@ -1261,13 +1277,13 @@ __device__ __forceinline__ void add_record(const float4 cm, bool useA, bool useB
 // at sixteen (64 registers, no spills; 33.7 vs 30.8 ms at twenty for a
 // 512-system ensemble). Against 256-thread CTAs at the same occupancy the
 // finer blocks shorten the uneven last wave (4.19 vs 4.28 ms at 2^20).
-template <bool COUNT, bool POT, bool SEG, bool GUARD>
+template <bool COUNT, bool POT, bool SEG, bool GUARD, bool HOST = false>
 __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel(
     const BHNode *__restrict__ nodes, const int *__restrict__ kids, const uint32_t *__restrict__ node_total,
     const float4 *__restrict__ pos, int64_t n, float eps2, float theta2, float dt, float4 *__restrict__ pos_out,
     float4 *__restrict__ vel, float4 *__restrict__ acc, float4 *__restrict__ force_out, const int *__restrict__ ids,
     unsigned long long *__restrict__ counters, float *__restrict__ phi_out, int euler, const int4 *__restrict__ work,
-    int nwork, const float4 *__restrict__ params, const uint32_t *__restrict__ P) {
+    int nwork, const float4 *__restrict__ params, const uint32_t *__restrict__ P, const HostOut host) {
     // One block of shared memory per warp, addressed from one base.
     struct __align__(16) WarpArea {
         int4 stk_i[kCellDepth];     // cell, mask A, mask B, -
@@ -1511,8 +1527,14 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
         }
         return;
     }
-    if (vA) integrate_sorted(bA, SEG ? pos[bA] : meA0, fx.x, fy.x, fz.x, dt, pos_out, vel, acc, force_out, ids, n, euler);
-    if (vB) integrate_sorted(bB, SEG ? pos[bB] : meB0, fx.y, fy.y, fz.y, dt, pos_out, vel, acc, force_out, ids, n, euler);
+    // HOST: a separate instance (even an unused store to the caller's arrays
+    // here added spills to the walk above).
+    if (vA)
+        integrate_sorted(bA, SEG ? pos[bA] : meA0, fx.x, fy.x, fz.x, dt, pos_out, vel, acc, force_out, ids, n, euler,
+                         HOST ? host : HostOut{});
+    if (vB)
+        integrate_sorted(bB, SEG ? pos[bB] : meB0, fx.y, fy.y, fz.y, dt, pos_out, vel, acc, force_out, ids, n, euler,
+                         HOST ? host : HostOut{});
 }
 
 // out[ids[i]] = in[i] (back to the caller's body order), positions with w = 0.
@@ -1807,18 +1829,29 @@ template <bool COUNT, bool POT, bool SEG, bool GUARD>
 void launch_walk(const BHWorkspace &w, unsigned blocks, cudaStream_t st, const uint32_t *node_total,
                  const float4 *pos, int64_t n, float eps2, float theta2, float dt, float4 *pos_out, float4 *vel,
                  float4 *acc, float4 *force_out, const int *ids, unsigned long long *counters, float *phi_out,
-                 int euler, const int4 *work, int nwork, const float4 *params, const uint32_t *P) {
+                 int euler, const int4 *work, int nwork, const float4 *params, const uint32_t *P,
+                 const HostOut &host = HostOut{}) {
+    if constexpr (!SEG && !POT) {
+        if (w.walk == kWalkCell && host.pos) {
+            cell_walk_kernel<COUNT, POT, SEG, GUARD, true><<<blocks * 4, 64, 0, st>>>(
+                w.nodes, w.kids, node_total, pos, n, eps2, theta2, dt, pos_out, vel, acc, force_out, ids, counters,
+                phi_out, euler, work, nwork, params, P, host);
+            return;
+        }
+    }
     if (w.walk == kWalkCell)
         cell_walk_kernel<COUNT, POT, SEG, GUARD><<<blocks * 4, 64, 0, st>>>(w.nodes, w.kids, node_total, pos, n, eps2,
                                                                          theta2, dt, pos_out, vel, acc, force_out,
                                                                          ids, counters, phi_out, euler, work, nwork,
-                                                                         params, P);
+                                                                         params, P, host);
     else
         traverse2_kernel<COUNT, POT, SEG, GUARD><<<blocks, 256, 0, st>>>(w.nodes, node_total, pos, n, eps2, theta2,
                                                                          dt, pos_out, vel, acc, force_out, ids,
                                                                          counters, phi_out, euler, work, nwork,
                                                                          params, P);
 }
+
+bool bh_walk_writes_host(const BHWorkspace &w) { return w.walk == kWalkCell && w.bodies_per_lane == 2; }
 
 int bh_walk_form() {
     const char *e = std::getenv("NBODY_BH_WALK");
@@ -1827,7 +1860,8 @@ int bh_walk_form() {
 
 cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,
                         float dt, float4 *pos_out, float4 *vel, float4 *acc, float4 *force_out, const int *ids,
-                        int euler, cudaStream_t st, StageTimer *timer) {
+                        int euler, cudaStream_t st, StageTimer *timer, const HostOut &host) {
+    if (host.pos && !bh_walk_writes_host(w)) return cudaErrorInvalidValue;
     if (timer) timer->begin(kStageTraverse, st);
     // The record count P[n] stays on the device; the kernel reads it.
     if (w.bodies_per_lane == 2) {
@@ -1836,15 +1870,15 @@ cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &
         if (w.counters)
             launch_walk<true, false, false, true>(w, blocks, st, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out, vel,
                                                  acc, force_out, ids, w.counters, nullptr, euler, nullptr, 0, nullptr,
-                                                 nullptr);
+                                                 nullptr, host);
         else if (eps2 > 0.f && theta2 > 0.f)
             launch_walk<false, false, false, false>(w, blocks, st, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out,
                                                    vel, acc, force_out, ids, nullptr, nullptr, euler, nullptr, 0,
-                                                   nullptr, nullptr);
+                                                   nullptr, nullptr, host);
         else
             launch_walk<false, false, false, true>(w, blocks, st, w.P + n, pos_sorted, n, eps2, theta2, dt, pos_out,
                                                   vel, acc, force_out, ids, nullptr, nullptr, euler, nullptr, 0,
-                                                  nullptr, nullptr);
+                                                  nullptr, nullptr, host);
     } else if (w.counters)
         traverse_kernel<true><<<grid_for(n, 256), 256, 0, st>>>(w.nodes, w.P + n, pos_sorted, n, eps2, theta2, dt,
                                                                 pos_out, vel, acc, force_out, ids, w.counters, euler);

@@ -102,13 +102,22 @@ bool bh_upsweep_by_levels(int64_t n, bool ensemble);
 int bh_upsweep_launches(int64_t n, bool ensemble);
 cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaStream_t st, int *status,
                      StageTimer *timer, const SegView &sv = SegView{});
+// The caller's arrays in the reference layout (device-mapped page-locked host
+// memory), written by the walk itself at index ids[b]: positions with w = 0,
+// velocities, accelerations and (if set) forces.
+struct HostOut {
+    float4 *pos = nullptr, *vel = nullptr, *acc = nullptr, *force = nullptr;
+};
+// Whether the workspace's walk form writes HostOut (the cell walk does).
+bool bh_walk_writes_host(const BHWorkspace &w);
 // Forces for every sorted body; with pos_out set, also the reference
 // integrator (pos_out must not alias pos_sorted). force_out, if set, receives
-// the acceleration at index ids[b] (or b when ids is null).
+// the acceleration at index ids[b] (or b when ids is null). host.pos set (and
+// bh_walk_writes_host): the new state also goes to the caller's arrays.
 // euler = 1 applies the GLSL path's semi-implicit Euler instead of the CPU order.
 cudaError_t bh_traverse(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,
                         float dt, float4 *pos_out, float4 *vel, float4 *acc, float4 *force_out, const int *ids,
-                        int euler, cudaStream_t st, StageTimer *timer);
+                        int euler, cudaStream_t st, StageTimer *timer, const HostOut &host = HostOut{});
 // Potential -sum m / sqrt(d^2 + eps^2) of every sorted body over the same
 // accepted records as the forces, into phi_out[ids[b]] (or phi_out[b]).
 cudaError_t bh_potential(const float4 *pos_sorted, int64_t n, const BHWorkspace &w, float eps2, float theta2,

@@ -190,7 +190,8 @@ int ensure_workspace(nbody_ctx *ctx, int64_t n) {
 // join: when set, the step waits for it before its gather and first merges
 // the masses in `masses4` (device, reference layout) into the positions,
 // which were copied in with w = 0 (the overlapped host step).
-int bh_step(nbody_ctx *ctx, cudaEvent_t join = nullptr, const float4 *masses4 = nullptr) {
+int bh_step(nbody_ctx *ctx, cudaEvent_t join = nullptr, const float4 *masses4 = nullptr,
+            const nbody::HostOut &host = nbody::HostOut{}) {
     nbody::BHWorkspace &w = ctx->ws;
     const int64_t n = ctx->n;
     float4 *P = ctx->pos[ctx->bh_pos], *Po = ctx->pos[ctx->bh_pos ^ 1];
@@ -209,8 +210,8 @@ int bh_step(nbody_ctx *ctx, cudaEvent_t join = nullptr, const float4 *masses4 = 
     NB_CK(ctx, nbody::bh_gather(n, w, P, V, A, I, Po, Vo, Ao, Io, ctx->stream, ctx->status, tm));
     NB_CK(ctx, nbody::bh_build(Po, n, w, ctx->stream, ctx->status, tm));
     // New positions go to the buffer the gather just read from.
-    NB_CK(ctx, nbody::bh_traverse(Po, n, w, ctx->eps2, ctx->theta2, ctx->dt, P, Vo, Ao, nullptr, nullptr,
-                                  ctx->integrator == NBODY_INTEGRATOR_GPU_EULER, ctx->stream, tm));
+    NB_CK(ctx, nbody::bh_traverse(Po, n, w, ctx->eps2, ctx->theta2, ctx->dt, P, Vo, Ao, nullptr, host.pos ? Io : nullptr,
+                                  ctx->integrator == NBODY_INTEGRATOR_GPU_EULER, ctx->stream, tm, host));
     ctx->bh_va ^= 1;
     ctx->ids_valid = true;
     return NBODY_OK;
@@ -472,10 +473,14 @@ namespace {
 // in first by a DMA copy (the reference layout's w = 0), velocities,
 // accelerations and masses by DMA copies on a side stream while the first
 // step's box, keys and sort run on the SMs; the step merges the masses into
-// the positions just before its gather, the first use of any of them. Same
-// values as nbody_upload + nbody_step.
+// the positions just before its gather, the first use of any of them. With
+// `host` set, the last step's walk writes the new state into the caller's
+// arrays as each body finishes (over the host link while the walk runs; the
+// inputs were copied in before). Same values as nbody_upload + nbody_step +
+// nbody_download.
 int bh_update_overlapped(nbody_ctx *ctx, const float *positions4, const float *velocities4,
-                         const float *accelerations4, const float *masses4, int steps) {
+                         const float *accelerations4, const float *masses4, int steps,
+                         const nbody::HostOut &host = nbody::HostOut{}) {
     DeviceGuard dg(ctx->device);
     int rc = ensure_workspace(ctx, ctx->n);
     if (rc != NBODY_OK) return rc;
@@ -497,8 +502,9 @@ int bh_update_overlapped(nbody_ctx *ctx, const float *positions4, const float *v
     ctx->bh_va = 0;
     ctx->ids_valid = false;
     ctx->uploaded = true;
-    rc = bh_step(ctx, ctx->ev_join, ctx->stage);
-    if (rc == NBODY_OK) rc = bh_steps(ctx, steps - 1);
+    rc = bh_step(ctx, ctx->ev_join, ctx->stage, steps == 1 ? host : nbody::HostOut{});
+    if (rc == NBODY_OK && steps > 1) rc = bh_steps(ctx, steps - 2);
+    if (rc == NBODY_OK && steps > 1) rc = bh_step(ctx, nullptr, nullptr, host);
     return rc;
 }
 
@@ -511,9 +517,22 @@ int nbody_update_host(nbody_ctx *ctx, float *positions4, float *velocities4, flo
         const size_t b4 = static_cast<size_t>(ctx->n) * sizeof(float4);
         const int dev = ctx->device;
         DeviceGuard dg(dev);
-        if (nbody::host_mapped(positions4, b4, dev) && nbody::host_mapped(velocities4, b4, dev) &&
-            nbody::host_mapped(accelerations4, b4, dev) && nbody::host_mapped(masses4, b4, dev)) {
-            int rc = bh_update_overlapped(ctx, positions4, velocities4, accelerations4, masses4, steps);
+        float4 *mp = nbody::host_mapped(positions4, b4, dev), *mv = nbody::host_mapped(velocities4, b4, dev),
+               *ma = nbody::host_mapped(accelerations4, b4, dev);
+        float4 *mf = forces4 ? nbody::host_mapped(forces4, b4, dev) : nullptr;
+        if (mp && mv && ma && nbody::host_mapped(masses4, b4, dev)) {
+            int rc = ensure_workspace(ctx, ctx->n);
+            if (rc != NBODY_OK) return rc;
+            if (nbody::bh_walk_writes_host(ctx->ws) && (!forces4 || mf)) {
+                nbody::HostOut host;
+                host.pos = mp;
+                host.vel = mv;
+                host.acc = ma;
+                host.force = mf;
+                rc = bh_update_overlapped(ctx, positions4, velocities4, accelerations4, masses4, steps, host);
+                return rc == NBODY_OK ? read_status(ctx) : rc;
+            }
+            rc = bh_update_overlapped(ctx, positions4, velocities4, accelerations4, masses4, steps);
             if (rc == NBODY_OK) rc = nbody_download(ctx, positions4, velocities4, accelerations4, forces4);
             return rc;
         }
