@@ -23,6 +23,30 @@
 #include "sort.h"
 #include "timer.h"
 
+// What a captured Barnes-Hut step depends on: a replay is valid while all of
+// it is unchanged (buffers, parameters, kernel forms, host arrays).
+struct GraphKey {
+    const void *ws = nullptr;
+    int64_t n = 0;
+    int va = -1, key_mode = -1, integrator = -1, walk = -1, bodies_per_lane = -1;
+    float dt = 0.f, eps2 = 0.f, theta2 = 0.f;
+    const void *host[9] = {};
+    bool operator==(const GraphKey &o) const {
+        if (ws != o.ws || n != o.n || va != o.va || key_mode != o.key_mode || integrator != o.integrator ||
+            walk != o.walk || bodies_per_lane != o.bodies_per_lane || dt != o.dt || eps2 != o.eps2 ||
+            theta2 != o.theta2)
+            return false;
+        for (int i = 0; i < 9; ++i)
+            if (host[i] != o.host[i]) return false;
+        return true;
+    }
+};
+
+struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    GraphKey key;
+};
+
 struct nbody_ctx {
     int device = 0;
     int mode = NBODY_MODE_PP;
@@ -66,6 +90,10 @@ struct nbody_ctx {
     // Side stream and events of the overlapped host step (made on first use).
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // Barnes-Hut steps replayed as CUDA graphs: the resident step by the
+    // parity of its velocity buffers, and the host step of nbody_update_host.
+    StepGraph graph_step[2], graph_host;
+    bool graphs_off = false;  // capture failed once (or NBODY_GRAPHS=0)
 };
 
 namespace {
@@ -217,9 +245,103 @@ int bh_step(nbody_ctx *ctx, cudaEvent_t join = nullptr, const float4 *masses4 = 
     return NBODY_OK;
 }
 
+GraphKey graph_key(const nbody_ctx *ctx) {
+    GraphKey k;
+    k.ws = ctx->ws_mem;
+    k.n = ctx->n;
+    k.va = ctx->bh_va;
+    k.key_mode = ctx->key_mode;
+    k.integrator = ctx->integrator;
+    k.walk = ctx->ws.walk;
+    k.bodies_per_lane = ctx->ws.bodies_per_lane;
+    k.dt = ctx->dt;
+    k.eps2 = ctx->eps2;
+    k.theta2 = ctx->theta2;
+    k.host[8] = reinterpret_cast<const void *>(static_cast<uintptr_t>(ctx->bh_pos + 1));
+    return k;
+}
+
+// Whether steps may run as graphs: not while per-stage timing or pair
+// counting is on (their launches differ), nor after a capture failed.
+bool graphs_usable(nbody_ctx *ctx) {
+    if (ctx->graphs_off || ctx->timer || ctx->ws.counters) return false;
+    const char *e = std::getenv("NBODY_GRAPHS");  // "0": launch every kernel directly
+    return !(e && std::strcmp(e, "0") == 0);
+}
+
+void drop_graph(StepGraph &g) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+}
+
+// Runs `body` (stream work on ctx->stream, possibly forking to ctx->side and
+// joining back) as the graph cached in g, capturing it first when g is empty
+// or was captured under another key. The host-side state that body changes
+// (buffer parities, id validity) is put back after a capture, so the caller
+// applies it once per replay. Returns NBODY_OK, or an error before anything
+// was launched, with *replayed = false when the caller should run body itself
+// (capture unavailable).
+template <class Body>
+int replay(nbody_ctx *ctx, StepGraph &g, const GraphKey &key, Body &&body, bool *replayed) {
+    *replayed = false;
+    if (!(g.exec && g.key == key)) {
+        drop_graph(g);
+        const int va = ctx->bh_va, pos = ctx->bh_pos, cur = ctx->cur;
+        const bool iv = ctx->ids_valid, up = ctx->uploaded;
+        if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->graphs_off = true;
+            return NBODY_OK;
+        }
+        const int rc = body();
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+        ctx->bh_va = va;
+        ctx->bh_pos = pos;
+        ctx->cur = cur;
+        ctx->ids_valid = iv;
+        ctx->uploaded = up;
+        if (rc != NBODY_OK || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            ctx->graphs_off = true;  // run this and later steps directly
+            return NBODY_OK;
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+            g.exec = nullptr;
+            cudaGetLastError();
+            ctx->graphs_off = true;
+            return NBODY_OK;
+        }
+        g.key = key;
+    }
+    NB_CK(ctx, cudaGraphLaunch(g.exec, ctx->stream));
+    *replayed = true;
+    return NBODY_OK;
+}
+
+// Steps on the resident state. From the second step after an upload (ids
+// valid, the same launches every step) each step is one graph launch, one
+// graph per parity of the velocity buffers: one host call instead of some
+// thirty, so a slow or busy host no longer leaves gaps between the step's
+// short kernels.
 int bh_steps(nbody_ctx *ctx, int steps) {
     int rc = ensure_workspace(ctx, ctx->n);
-    for (int s = 0; rc == NBODY_OK && s < steps; ++s) rc = bh_step(ctx);
+    for (int s = 0; rc == NBODY_OK && s < steps; ++s) {
+        if (ctx->ids_valid && graphs_usable(ctx)) {
+            bool replayed = false;
+            rc = replay(ctx, ctx->graph_step[ctx->bh_va], graph_key(ctx), [&] { return bh_step(ctx); }, &replayed);
+            if (rc != NBODY_OK) break;
+            if (replayed) {
+                ctx->bh_va ^= 1;
+                ctx->ids_valid = true;
+                continue;
+            }
+        }
+        rc = bh_step(ctx);
+    }
     return rc;
 }
 
@@ -324,6 +446,9 @@ int nbody_destroy(nbody_ctx *ctx) {
         cudaFree(ctx->diag_mem);
         cudaFree(ctx->diag_phi);
         delete ctx->timer;
+        drop_graph(ctx->graph_step[0]);
+        drop_graph(ctx->graph_step[1]);
+        drop_graph(ctx->graph_host);
         if (ctx->side) cudaStreamDestroy(ctx->side);
         if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
         if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
@@ -490,19 +615,44 @@ int bh_update_overlapped(nbody_ctx *ctx, const float *positions4, const float *v
         NB_CK(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
     }
     const size_t b4 = static_cast<size_t>(ctx->n) * sizeof(float4);
-    NB_CK(ctx, cudaEventRecord(ctx->ev_fork, ctx->stream));
-    NB_CK(ctx, cudaMemcpyAsync(ctx->pos[0], positions4, b4, cudaMemcpyHostToDevice, ctx->stream));
-    NB_CK(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-    NB_CK(ctx, cudaMemcpyAsync(ctx->vel, velocities4, b4, cudaMemcpyHostToDevice, ctx->side));
-    NB_CK(ctx, cudaMemcpyAsync(ctx->acc, accelerations4, b4, cudaMemcpyHostToDevice, ctx->side));
-    NB_CK(ctx, cudaMemcpyAsync(ctx->stage, masses4, b4, cudaMemcpyHostToDevice, ctx->side));
-    NB_CK(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
-    ctx->cur = 0;
-    ctx->bh_pos = 0;
-    ctx->bh_va = 0;
-    ctx->ids_valid = false;
-    ctx->uploaded = true;
-    rc = bh_step(ctx, ctx->ev_join, ctx->stage, steps == 1 ? host : nbody::HostOut{});
+    const nbody::HostOut first_out = steps == 1 ? host : nbody::HostOut{};
+    // The copies in and the first step: the same launches on every call with
+    // the same arrays, so they replay as one graph.
+    auto first = [&]() -> int {
+        NB_CK(ctx, cudaEventRecord(ctx->ev_fork, ctx->stream));
+        NB_CK(ctx, cudaMemcpyAsync(ctx->pos[0], positions4, b4, cudaMemcpyHostToDevice, ctx->stream));
+        NB_CK(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+        NB_CK(ctx, cudaMemcpyAsync(ctx->vel, velocities4, b4, cudaMemcpyHostToDevice, ctx->side));
+        NB_CK(ctx, cudaMemcpyAsync(ctx->acc, accelerations4, b4, cudaMemcpyHostToDevice, ctx->side));
+        NB_CK(ctx, cudaMemcpyAsync(ctx->stage, masses4, b4, cudaMemcpyHostToDevice, ctx->side));
+        NB_CK(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
+        ctx->cur = 0;
+        ctx->bh_pos = 0;
+        ctx->bh_va = 0;
+        ctx->ids_valid = false;
+        ctx->uploaded = true;
+        return bh_step(ctx, ctx->ev_join, ctx->stage, first_out);
+    };
+    bool replayed = false;
+    if (graphs_usable(ctx)) {
+        NB_CK(ctx, nbody::sort_prepare(ctx->device));  // launch attributes before any capture
+        GraphKey key = graph_key(ctx);
+        key.va = 0;
+        const void *arrays[9] = {positions4, velocities4, accelerations4, masses4, first_out.pos, first_out.vel,
+                                 first_out.acc, first_out.force, nullptr};
+        for (int i = 0; i < 9; ++i) key.host[i] = arrays[i];
+        rc = replay(ctx, ctx->graph_host, key, first, &replayed);
+        if (rc != NBODY_OK) return rc;
+    }
+    if (replayed) {  // the state the first step leaves
+        ctx->cur = 0;
+        ctx->bh_pos = 0;
+        ctx->bh_va = 1;
+        ctx->ids_valid = true;
+        ctx->uploaded = true;
+    } else {
+        rc = first();
+    }
     if (rc == NBODY_OK && steps > 1) rc = bh_steps(ctx, steps - 2);
     if (rc == NBODY_OK && steps > 1) rc = bh_step(ctx, nullptr, nullptr, host);
     return rc;
