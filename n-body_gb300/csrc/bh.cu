@@ -1286,12 +1286,12 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
     int nwork, const float4 *__restrict__ params, const uint32_t *__restrict__ P, const HostOut host) {
     // One block of shared memory per warp, addressed from one base.
     struct __align__(16) WarpArea {
-        int4 stk_i[kCellDepth];     // cell, mask A, mask B, -
+        int4 stk_i[kCellDepth];     // cell, mask A, mask B, box hz (float bits)
         float4 stk_lo[kCellDepth];  // box: lx, ly, lz, hx
-        float2 stk_hi[kCellDepth];  // box: hy, hz
+        float stk_hy[kCellDepth];   // box: hy
         int4 bat_i[4];              // the cells of a round, as popped
         float4 bat_lo[4];
-        float2 bat_hi[4];
+        float bat_hy[4];
         float4 ch_cm[32];           // the round's children's cm, by the lane that loaded them
     };
     __shared__ WarpArea area[kCellWarps];
@@ -1301,10 +1301,10 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
     const int lane = threadIdx.x & 31;
     int4 *si = A.stk_i;
     float4 *slo = A.stk_lo;
-    float2 *shi = A.stk_hi;
+    float *shy = A.stk_hy;
     int4 *bi = A.bat_i;
     float4 *blo = A.bat_lo;
-    float2 *bhi = A.bat_hi;
+    float *bhy = A.bat_hy;
     float4 *ccm = A.ch_cm;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     int64_t base, end;
@@ -1396,9 +1396,9 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
         if (sp < kCellDepth) {
             const SetBox b = box_of(oa, ob, lane, meA0, meB0);
             if (lane == 0) {
-                si[sp] = make_int4(k, static_cast<int>(oa), static_cast<int>(ob), 0);
+                si[sp] = make_int4(k, static_cast<int>(oa), static_cast<int>(ob), __float_as_int(b.hz));
                 slo[sp] = make_float4(b.lx, b.ly, b.lz, b.hx);
-                shi[sp] = make_float2(b.hy, b.hz);
+                shy[sp] = b.hy;
             }
             ++sp;
         } else {
@@ -1426,19 +1426,19 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
         if (grp < nb) {
             const int4 t = si[sp + grp];
             const float4 bl = slo[sp + grp];
-            const float2 bh = shi[sp + grp];
+            const float hy = shy[sp + grp];
             if ((lane & 7) == 0) {
                 bi[grp] = t;
                 blo[grp] = bl;
-                bhi[grp] = bh;
+                bhy[grp] = hy;
             }
             SetBox box;
             box.lx = bl.x;
             box.ly = bl.y;
             box.lz = bl.z;
             box.hx = bl.w;
-            box.hy = bh.x;
-            box.hz = bh.y;
+            box.hy = hy;
+            box.hz = __int_as_float(t.w);
             kid = __ldg(&kids[8 * static_cast<int64_t>(t.x) + (lane & 7)]);
             if (kid >= 0) {
                 const float4 cm = __ldg(&nodes[kid].cm);
@@ -1460,9 +1460,9 @@ __global__ void __launch_bounds__(64, (COUNT || SEG) ? 16 : 24) cell_walk_kernel
                 const int k = __shfl_sync(0xffffffffu, kid, __ffs(m) - 1);
                 if (sp < kCellDepth) {
                     if (lane == 0) {
-                        si[sp] = make_int4(k, static_cast<int>(sa), static_cast<int>(sb), 0);
+                        si[sp] = make_int4(k, static_cast<int>(sa), static_cast<int>(sb), t.w);
                         slo[sp] = blo[q];
-                        shi[sp] = bhi[q];
+                        shy[sp] = bhy[q];
                     }
                     ++sp;
                 } else {
