@@ -658,11 +658,64 @@ int bh_update_overlapped(nbody_ctx *ctx, const float *positions4, const float *v
     return rc;
 }
 
+// nbody_update_host for one direct-sum step with page-locked arrays: the
+// gather kernel in, the step and the scatter kernel out replay as one graph
+// (the same launches on every call with the same arrays). Returns false, with
+// nothing launched, when the call does not qualify; else *rc is the call's
+// status.
+bool pp_update_graphed(nbody_ctx *ctx, const float *positions4, float *velocities4, float *accelerations4,
+                       const float *masses4, float *forces4, int *rc) {
+    DeviceGuard dg(ctx->device);
+    if (!graphs_usable(ctx)) return false;
+    const size_t b4 = static_cast<size_t>(ctx->n) * sizeof(float4);
+    const int dev = ctx->device;
+    float4 *mp = nbody::host_mapped(positions4, b4, dev), *mv = nbody::host_mapped(velocities4, b4, dev),
+           *ma = nbody::host_mapped(accelerations4, b4, dev), *mm = nbody::host_mapped(masses4, b4, dev);
+    float4 *mf = forces4 ? nbody::host_mapped(forces4, b4, dev) : nullptr;
+    if (!(mp && mv && ma && mm && (!forces4 || mf))) return false;
+    const nbody::PPPlan plan = nbody::pp_plan(ctx->n, ctx->device);
+    *rc = ensure_scratch(ctx, plan.partial_bytes);  // allocation stays outside the capture
+    if (*rc != NBODY_OK) return true;
+    auto body = [&]() -> int {
+        NB_CK(ctx, nbody::host_gather(mp, mm, mv, ma, ctx->pos[0], ctx->vel, ctx->acc, ctx->n, ctx->stream));
+        nbody::Integrate g;
+        g.pos_out = ctx->pos[1];
+        g.vel = ctx->vel;
+        g.acc = ctx->acc;
+        g.dt = ctx->dt;
+        g.euler = ctx->integrator == NBODY_INTEGRATOR_GPU_EULER;
+        NB_CK(ctx, nbody::pp_launch(plan, ctx->pos[0], ctx->n, ctx->eps2, g, ctx->scratch, ctx->stream, ctx->status,
+                                    nullptr));
+        NB_CK(ctx, nbody::host_scatter(ctx->pos[1], ctx->vel, ctx->acc, nullptr, nullptr, mp, mv, ma, mf, nullptr,
+                                       ctx->n, ctx->stream, ctx->status));
+        return NBODY_OK;
+    };
+    GraphKey key = graph_key(ctx);
+    key.ws = ctx->scratch;
+    const void *arrays[9] = {mp, mv, ma, mm, mf, nullptr, nullptr, nullptr, nullptr};
+    for (int i = 0; i < 9; ++i) key.host[i] = arrays[i];
+    bool replayed = false;
+    *rc = replay(ctx, ctx->graph_host, key, body, &replayed);
+    if (*rc != NBODY_OK) return true;
+    if (!replayed) return false;  // capture unavailable: the caller's path runs the call
+    ctx->cur = 1;  // the step's new state is in pos[1]
+    ctx->bh_pos = 0;
+    ctx->bh_va = 0;
+    ctx->ids_valid = false;
+    ctx->uploaded = true;
+    *rc = read_status(ctx);
+    return true;
+}
+
 }  // namespace
 
 int nbody_update_host(nbody_ctx *ctx, float *positions4, float *velocities4, float *accelerations4,
                       const float *masses4, float *forces4, int steps) {
     if (!ctx || !positions4 || !velocities4 || !accelerations4 || !masses4 || steps < 0) return NBODY_ERR_ARG;
+    if (ctx->mode == NBODY_MODE_PP && steps == 1) {
+        int rc = NBODY_OK;
+        if (pp_update_graphed(ctx, positions4, velocities4, accelerations4, masses4, forces4, &rc)) return rc;
+    }
     if (ctx->mode == NBODY_MODE_BH && steps >= 1) {
         const size_t b4 = static_cast<size_t>(ctx->n) * sizeof(float4);
         const int dev = ctx->device;

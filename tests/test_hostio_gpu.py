@@ -185,22 +185,23 @@ def test_partly_page_locked_buffer_takes_the_copy_path(nb, cuda):
         assert int(cudart.cudaHostUnregister(ptr)) == 0
 
 
+@pytest.mark.parametrize("mode,n", [("bh", 30_000), ("pp", 5_000)])
 @pytest.mark.parametrize("pinned", ["all", "none"])
-def test_graph_replayed_steps_match_direct_launches(nb, cuda, monkeypatch, pinned):
-    """Barnes-Hut steps replayed as CUDA graphs (the resident step by buffer
-    parity, the page-locked host step as one graph with its copies) give the
-    same bits as the same steps launched kernel by kernel (NBODY_GRAPHS=0),
-    over calls that replay a captured graph several times."""
+def test_graph_replayed_steps_match_direct_launches(nb, cuda, monkeypatch, pinned, mode, n):
+    """Steps replayed as CUDA graphs give the same bits as the same steps
+    launched kernel by kernel (NBODY_GRAPHS=0), over calls that replay a
+    captured graph several times: for Barnes-Hut the resident step (one graph
+    per buffer parity) and the page-locked host step with its copies, for the
+    direct sum the page-locked host call (gather, step, scatter)."""
     torch = cuda
     from nbody_gb300 import initializers as I
 
-    n = 30_000
     pos, vel, mass = I.plummer(n, a=50.0, seed=5)
     out = {}
     for graphs in ("1", "0"):
         monkeypatch.setenv("NBODY_GRAPHS", graphs)
         s = _system(nb, torch, pos, vel, mass, pinned)
-        solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode="bh", theta2=0.25)
+        solver = nb.ParticleSolverCUDA(0.0035, 40.0, n, mode=mode, theta2=0.25)
         for _ in range(3):
             solver.update_particle_positions(s)  # host arrays in and out
         solver.update_particle_positions(s, steps=4)
