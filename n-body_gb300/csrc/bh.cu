@@ -1206,14 +1206,14 @@ __device__ __forceinline__ int certify(const float4 cm, const int4 meta, const S
     const float gx = fmaxf(fmaxf(__fsub_rn(b.lx, cm.x), __fsub_rn(cm.x, b.hx)), 0.f);
     const float gy = fmaxf(fmaxf(__fsub_rn(b.ly, cm.y), __fsub_rn(cm.y, b.hy)), 0.f);
     const float gz = fmaxf(fmaxf(__fsub_rn(b.lz, cm.z), __fsub_rn(cm.z, b.hz)), 0.f);
+    const float lo2 = __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
+    if (s2 < __fmul_rn(theta2, lo2)) return 0;
+    if (meta.w != 0) return 2;
     const float ux = fmaxf(fabsf(__fsub_rn(cm.x, b.lx)), fabsf(__fsub_rn(b.hx, cm.x)));
     const float uy = fmaxf(fabsf(__fsub_rn(cm.y, b.ly)), fabsf(__fsub_rn(b.hy, cm.y)));
     const float uz = fmaxf(fabsf(__fsub_rn(cm.z, b.lz)), fabsf(__fsub_rn(b.hz, cm.z)));
-    const float lo2 = __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
     const float hi2 = __fadd_rn(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)), __fmul_rn(uz, uz));
-    if (s2 < __fmul_rn(theta2, lo2)) return 0;
-    if (meta.w == 0 && !(s2 < __fmul_rn(theta2, hi2))) return 1;
-    return 2;
+    return s2 < __fmul_rn(theta2, hi2) ? 2 : 1;
 }
 
 // ------------------------------------------------------------ cell walk
