@@ -950,9 +950,8 @@ __device__ __forceinline__ void direct_sum_range(const float4 *__restrict__ pos,
     }
 }
 
-// Body b's new state into the caller's arrays at its caller index (out of
-// line: the walk instance that calls it spills 140 bytes, 164 with it inline).
-__device__ __noinline__ void write_host(const HostOut host, const int *__restrict__ ids, int64_t b, int64_t n,
+// Body b's new state into the caller's arrays at its caller index.
+__device__ __forceinline__ void write_host(const HostOut host, const int *__restrict__ ids, int64_t b, int64_t n,
                                         float4 p, float4 v, float4 a) {
     const int d = ids ? ids[b] : static_cast<int>(b);
     if (d < 0 || d >= n) return;
