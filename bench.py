@@ -458,11 +458,11 @@ def bench_bh(args, world, rank, local, dist):
     e2e = {"value": float(n) * e2e_steps * world / e2e_s, "unit": "body-steps/s", "h2d_bytes_per_step": 4 * 16 * n,
            "d2h_bytes_per_step": 4 * 16 * n, "ms_per_step": round(e2e_s * 1e3 / e2e_steps, 3), "steps": e2e_steps,
            "api": "nbody_update_host (ParticleSolver::updateParticlePositions)"}
-    # bbox, keys, sort (histogram, scan, 8 passes), gather, 8 build kernels and
+    # bbox, keys, sort (histogram, scan, 8 passes), gather, 7 build kernels and
     # the child table of the cell walk, the upsweep (one climbing launch below
     # 2^21 bodies; from there bucket centres, level count, level scatter and one
     # launch per octree level: 24), walk
-    launches_per_step = 22 + (0 if os.environ.get("NBODY_BH_WALK") == "union" else 1) + \
+    launches_per_step = 21 + (0 if os.environ.get("NBODY_BH_WALK") == "union" else 1) + \
         (1 if n < (1 << 21) else 24)
     line = {"metric": METRIC, "component": "BH body-steps/s", "value": value, "unit": "body-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,

@@ -380,7 +380,8 @@ __device__ __forceinline__ int delta_at(const uint64_t *__restrict__ k, const in
     return base + 63 + __clz(static_cast<int>(i ^ j));                        // equal keys: break ties by index
 }
 
-__global__ void radix_tree_kernel(const uint64_t *__restrict__ k, int64_t n, BinaryTree t, SegView sv) {
+__global__ void radix_tree_kernel(const uint64_t *__restrict__ k, int64_t n, BinaryTree t, SegView sv,
+                                  uint32_t *__restrict__ mask, int base) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     const int *seg = sv.seg;
@@ -412,17 +413,16 @@ __global__ void radix_tree_kernel(const uint64_t *__restrict__ k, int64_t n, Bin
     if (left < 0) t.lparent[~left] = static_cast<int>(i); else t.iparent[left] = static_cast<int>(i);
     if (right < 0) t.lparent[~right] = static_cast<int>(i); else t.iparent[right] = static_cast<int>(i);
     if (i == 0) t.iparent[0] = -1;
-}
-
-// Cell tops: radix-tree nodes whose octree level exceeds their parent's.
-__global__ void mark_cells_kernel(int64_t n, BinaryTree t, uint32_t *__restrict__ mask, int base) {
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
-    const int L = level_c(t.delta[i], base);
-    const int Lp = i == 0 ? -1 : level_c(t.delta[t.iparent[i]], base);
+    // Cell top: a node whose octree level exceeds its parent's. A node is the
+    // maximal range sharing its prefix, so its parent extends it across the
+    // end whose neighbour is the more similar one, and the parent's delta is
+    // the larger of the deltas across the two ends (-1 past the array).
+    const int L = level_c(dnode, base);
+    const int dp = i == 0 ? -1 : max(delta_at(k, seg, n, lo, lo - 1), delta_at(k, seg, n, hi, hi + 1));
+    const int Lp = i == 0 ? -1 : level_c(dp, base);
     const bool top = L > Lp;
     t.top[i] = top ? 1 : 0;
-    if (top) atomicOr(&mask[t.lo[i]], 1u << L);
+    if (top) atomicOr(&mask[lo], 1u << L);
 }
 
 __global__ void count_nodes_kernel(const uint64_t *__restrict__ k, int64_t n, const uint32_t *__restrict__ mask,
@@ -1793,8 +1793,7 @@ cudaError_t bh_build(const float4 *pos_sorted, int64_t n, BHWorkspace &w, cudaSt
     cudaError_t e = cudaMemsetAsync(w.mask, 0, sizeof(uint32_t) * static_cast<size_t>(n), st);
     if (e != cudaSuccess) return e;
     if (n >= 2) {
-        radix_tree_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(k, n, w.tree, sv);
-        mark_cells_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(n, w.tree, w.mask, sv.seg ? 32 : 0);
+        radix_tree_kernel<<<grid_for(n - 1, 256), 256, 0, st>>>(k, n, w.tree, sv, w.mask, sv.seg ? 32 : 0);
     }
     count_nodes_kernel<<<grid_for(n, 256), 256, 0, st>>>(k, n, w.mask, w.cnt, sv);
     const int tiles = static_cast<int>((n + kScanTile - 1) / kScanTile);

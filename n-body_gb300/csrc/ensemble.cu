@@ -780,11 +780,11 @@ int nbody_ensemble_counts(nbody_ensemble *e, int *systems, int64_t *pp_bodies, i
     if (bh_bodies) *bh_bodies = e->bh_n;
     if (launches_per_step) {
         // direct sum: 1; Barnes-Hut: bbox, keys, histogram + scan + 8 key
-        // passes, segment keys + histogram + scan + passes, gather, 8 build
+        // passes, segment keys + histogram + scan + passes, gather, 7 build
         // kernels (+ the cell walk's child table), the upsweep's, traversal
         int l = e->pp_nitems > 0 ? 1 : 0;
         if (e->bh_n > 0)
-            l += 2 + (2 + 8) + (e->tab.systems > 1 ? 3 + e->tab.seg_passes : 0) + 1 + 8 +
+            l += 2 + (2 + 8) + (e->tab.systems > 1 ? 3 + e->tab.seg_passes : 0) + 1 + 7 +
                  (e->ws.walk == nbody::kWalkCell ? 1 : 0) + nbody::bh_upsweep_launches(e->bh_n, true) + 1;
         *launches_per_step = l;
     }
